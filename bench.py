@@ -1,0 +1,354 @@
+"""Benchmark of the GB300 SES3D time step: GLL point-steps/s on the plain 3-D forward
+workload (96 x 96 x 40 elements, lpd 4: 46.08M GLL points; anelastic, PML 3, one
+moment-tensor source, 200 receivers), synthetic seeded inputs.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One JSON line on rank 0. `value` is device-timed (CUDA events on the library's
+stream) whole-job throughput with the model resident in HBM; `e2e` is the same
+metric through the public API (Simulation: create, model upload from pinned host
+memory, K steps, seismogram download), host clock around all of it. The field
+state (36 floats x 46.08M points = 6.6 GB) exceeds the 129 MB L2 many times over,
+so no L2 flush is needed between steps. With --gpus N > 1 (torchrun) every rank
+runs an independent replica of the workload on its own GPU (the solver shards by
+event, not by domain: replicas only); value = all ranks' points x steps / max time.
+--impl reference times the CPU restatement of the reference solver (the oracle,
+FP32, OpenMP on all host cores) on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GLL point-steps/s"
+# Algorithmic bytes per local GLL node and iteration (forward, anelastic, 3 SLS, FP32):
+# element-local state 36 floats read+write (288 B) + 6 material floats (24 B) + per unique
+# node v read+write and 1/M read (28 B x unique/local ratio).
+STATE_B, MAT_B, UNIQ_B = 288.0, 24.0, 28.0
+# k_element alone: state + material + v gather (12 B x ratio).
+ELEM_UNIQ_B = 12.0
+
+
+def load_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic(workload):
+    """dram bytes per k_element launch from the committed ncu summary (null if absent)."""
+    path = os.path.join(ROOT, "profiles", "k_element_%s_traffic.json" % workload)
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not self.path:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        pw = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        load = [s for s, p in zip(sm, pw) if p > 0.25 * max(pw)] if pw else sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(load or sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(pw) if pw else None, "samples": len(rows), "reasons": reasons}
+
+
+def dist_init(n_gpus):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(problem, steps):
+    """The oracle (CPU restatement of the reference, FP32, all host cores) on `steps`
+    iterations of the same workload; set-up excluded."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    o = oracle.Oracle(problem)
+    o.run(1)  # first iteration touches every page: untimed warm-up
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": problem.n_nodes * steps / dt, "unit": METRIC, "cores": int(os.environ["OMP_NUM_THREADS"]),
+            "kind": "port", "sample": "%d time steps of the %s workload (%d GLL points), after one untimed "
+                                      "step; set-up excluded" % (steps, problem.label, problem.n_nodes)}
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+    from ses3d_gb300 import build as B
+    from ses3d_gb300 import synth
+    from ses3d_gb300.solver import Simulation
+
+    if rank == 0 or not os.path.exists(B.LIB):
+        B.build()
+    barrier(world)
+    nt = args.warmup + args.steps + 8  # the block-shape autotune spends 6 of the warm-up steps
+    p = synth.make_problem(args.workload, nt=nt, seed=args.seed)
+    N = p.n_nodes
+    ex, ey, ez = p.nx + 1, p.ny + 1, p.nz + 1
+    G = (4 * ex + 1) * (4 * ey + 1) * (4 * ez + 1)
+    r_u = G / N
+    sim = Simulation.from_problem(p)
+    if args.epb:
+        sim.set_block_elements(args.epb)
+    else:  # autotune the element-kernel block shape on a few steps
+        best = None
+        for epb in (1, 2, 4):
+            sim.set_block_elements(epb)
+            sim.profile(True)
+            sim.step(2)
+            ms, n = sim.kernel_time("element")
+            if best is None or ms / n < best[1]:
+                best = (epb, ms / n)
+        sim.profile(False)
+        sim.set_block_elements(best[0])
+        args.epb = best[0]
+    if args.graph:
+        sim.use_graph(True, args.graph)
+    # warm-up (the autotune steps above count towards it)
+    remaining_warm = max(0, args.warmup - sim.it)
+    sim.step(remaining_warm)
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(sim.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = sim.launch_count
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        sim.step(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    launches = sim.launch_count - launches0
+    clocks = clk.summary()
+    ms_max = max_over_ranks(ms, world)
+    value = world * N * args.steps / (ms_max / 1e3)
+    steps_done = sim.it
+    seis = sim.seismograms(0)
+    finite = bool(np.all(np.isfinite(seis[0]))) and bool(np.all(np.isfinite(sim.vmax())))
+    sim.close()
+
+    # dominant kernel, timed live with CUDA events on the library's stream (eager launches)
+    prof = Simulation.from_problem(p)
+    prof.set_block_elements(args.epb)
+    prof.step(2)
+    prof.profile(True)
+    prof.step(args.prof_steps)
+    el_ms, el_n = prof.kernel_time("element")
+    nd_ms, nd_n = prof.kernel_time("node")
+    rc_ms, rc_n = prof.kernel_time("receivers")
+    prof.close()
+    el_avg = el_ms / max(el_n, 1)
+    elem_bytes = N * (STATE_B + MAT_B + ELEM_UNIQ_B * r_u)
+    peak, peak_kind = load_peak()
+    achieved = elem_bytes / (el_avg / 1e3) / 1e9
+    tr = load_traffic(args.workload)
+    step_bytes = N * (STATE_B + MAT_B + UNIQ_B * r_u)
+    step_gbs = step_bytes / (ms / args.steps / 1e3) / 1e9
+
+    # end to end through the public API with host buffers (pinned)
+    e2e = None
+    if not args.no_e2e:
+        pinned = {}
+        for k, v in p.model.items():
+            t = torch.empty(v.size, dtype=torch.float32, pin_memory=True)
+            t.numpy()[:] = v
+            pinned[k] = t.numpy()
+        ev = p.events[0]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cfg_sim = Simulation.from_problem(p, nt=args.steps, model=False)
+        cfg_sim.set_model(pinned)
+        cfg_sim.step(args.steps)
+        out = cfg_sim.seismograms(0)
+        t1 = time.perf_counter()
+        nr = cfg_sim.n_receivers(0)
+        cfg_sim.close()
+        t_e2e = max_over_ranks(t1 - t0, world)
+        h2d = sum(a.nbytes for a in pinned.values()) + 4 * args.steps + ev.receivers.loc.nbytes + 24
+        d2h = sum(o.nbytes for o in out)
+        e2e = {"value": world * N * args.steps / t_e2e, "unit": METRIC,
+               "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+               "seconds": t_e2e, "includes": "create + model upload + %d steps + seismogram download" % args.steps}
+        del pinned
+
+    res = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "%s: plain 3-D forward, %dx%dx%d elements, lpd 4, %d GLL points, anelastic "
+                               "(3 SLS), PML 3, 1 moment-tensor source, %d receivers" %
+                               (args.workload, ex, ey, ez, N, len(p.events[0].receivers.names)),
+                   "gll_points": N, "unique_nodes": G, "elements_per_cta": args.epb,
+                   "graph_steps": args.graph, "l2": "inputs larger than L2 (6.6 GB state), no flush",
+                   "step_algorithmic_bytes_per_point": STATE_B + MAT_B + UNIQ_B * r_u,
+                   "step_achieved_gbs": step_gbs, "step_frac_of_peak": step_gbs / peak,
+                   "finite": finite, "steps_completed": steps_done,
+                   "kernel_ms": {"k_element": el_avg, "k_node": nd_ms / max(nd_n, 1),
+                                 "k_receivers": rc_ms / max(rc_n, 1)}},
+        "roofline": {"bound": "hbm", "kernel": "k_element", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "algorithmic_bytes_per_launch": elem_bytes,
+                     "traffic": (tr or {}).get("dram_bytes_per_launch_full") if tr else None},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if e2e:
+        res["e2e"] = e2e
+    if rank == 0 and world == 1 and not args.no_cpu:
+        res["cpu_baseline"] = cpu_baseline(p, args.cpu_steps)
+    return res
+
+
+def run_reference(args, rank, world):
+    from ses3d_gb300 import synth
+    if rank != 0:
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    steps = max(1, min(args.steps, args.cpu_steps))
+    warm = max(1, min(args.warmup, 1))
+    p = synth.make_problem(args.workload, nt=steps + warm + 1, seed=args.seed)
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    o = oracle.Oracle(p)
+    o.run(warm)
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    v = p.n_nodes * steps / dt
+    sample = ("%d time steps (after %d untimed) of the %s workload, %d GLL points, CPU restatement of the "
+              "reference (FP32, OpenMP)" % (steps, warm, args.workload, p.n_nodes))
+    return {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world, "steps": steps, "warmup": warm,
+            "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "gll_points": p.n_nodes},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": int(os.environ["OMP_NUM_THREADS"]),
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2")
+    ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--epb", type=int, default=0, help="elements per CTA (0: autotune)")
+    ap.add_argument("--graph", type=int, default=10, help="steps per CUDA graph (0: eager)")
+    ap.add_argument("--prof-steps", type=int, default=10)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+        res = run_reference(args, rank, world)
+    else:
+        rank, world, local = dist_init(args.gpus)
+        res = run_ours(args, rank, world, local)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,226 @@
+/*
+ * ses3d_gpu.h -- C ABI of the GB300 SES3D time-stepping library (libses3d_gpu.so).
+ *
+ * The reference solver has no library interface: its hot path is a set of
+ * argument-less Fortran subroutines that mutate `module variables`
+ * (SOURCE/ses3d_modules.f90:33-233) and are called in a fixed order by
+ * `program ses3d_main` (SOURCE/ses3d_main.f90:77-180). Each entry point below
+ * replaces one of those subroutines (or the part of one that touches the hot
+ * path) and states which. A Fortran driver binds them with ISO_C_BINDING; the
+ * Python package binds them with ctypes.
+ *
+ * Conventions
+ *  - Every entry point returns 0 on success or a negative SES3D_E* code;
+ *    ses3d_gpu_last_error() gives a message for the last failure on a handle.
+ *  - Host arrays are caller-owned and only read/written during the call.
+ *    Arrays use the reference layout: Fortran column-major
+ *    (i,j,k,in,jn,kn), element index i fastest, exactly the records of
+ *    MODELS/MODELS/<name><rank> and of the ofd/ffd output files.
+ *  - The library owns all device memory of a handle. One handle per
+ *    (process, device); calls on one handle are not thread-safe.
+ *  - Several events that share one mesh and model run together in one handle
+ *    (config.n_events > 1): every time step is one launch sequence for all of
+ *    them. `event` arguments are 0-based.
+ *  - All field arithmetic is FP32 as in the reference; the Frechet-kernel
+ *    time integrals accumulate in FP64.
+ */
+#ifndef SES3D_GPU_H
+#define SES3D_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SES3D_OK 0
+#define SES3D_E_CONFIG (-1)   /* invalid configuration or argument */
+#define SES3D_E_OOM (-2)      /* device allocation failed */
+#define SES3D_E_CUDA (-3)     /* CUDA runtime error */
+#define SES3D_E_STATE (-4)    /* call out of order (e.g. step before set_model) */
+#define SES3D_E_NAN (-5)      /* non-finite wavefield detected by the watchdog */
+#define SES3D_E_NOTFOUND (-6) /* source/receiver outside the box */
+#define SES3D_E_NODEV (-7)    /* no CUDA device */
+
+typedef struct ses3d_gpu ses3d_gpu;
+
+/* Run configuration: the values ses3d_input reads from the boxfile, the setup,
+ * event and relax files (SOURCE/ses3d_input.f90:44-357), plus the reference's
+ * compile-time `pml` (SOURCE/ses3d_modules.f90:21), here a run-time value. */
+typedef struct {
+  int32_t nx, ny, nz;     /* elements - 1 in x (colatitude), y (longitude), z (radius) */
+  int32_t lpd;            /* Lagrange degree; this library implements lpd = 4 */
+  int32_t pml;            /* PML width in elements (reference default 2) */
+  int32_t is_diss;        /* 1: anelastic (3 SLS mechanisms), 0: elastic */
+  int32_t adjoint_flag;   /* 0 forward, 1 forward + store, 2 adjoint + kernels */
+  int32_t samp_ad;        /* forward-field storing rate */
+  int32_t nt;             /* time steps */
+  int32_t n_events;       /* events sharing this mesh (1 = plain run) */
+  int32_t grad_variant;   /* 0: SOURCE/ses3d_grad.f90, 1: SOURCE/ses3d_grad_Q.f90 */
+  int32_t reserved;
+  float dt;
+  float xmin, xmax, ymin, ymax; /* box, radians (boxfile physical boundaries) */
+  float zmin, zmax;             /* box radii, m */
+  float zmax_global;            /* setup z_max, m (depths are measured from it) */
+  float tau_p[3], D_p[3];       /* relax file */
+} ses3d_config;
+
+/* Library version string. */
+const char *ses3d_gpu_version(void);
+
+/* Creates a handle: GLL tables, geometry, PML profiles and all device buffers.
+ * Replaces the geometry part of ses3d_init (SOURCE/ses3d_init.f90:87-248,574-709). */
+int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out);
+
+/* Frees every resource of the handle. */
+int ses3d_gpu_destroy(ses3d_gpu *h);
+
+/* Message for the last failure on h (or for the last failed create if h is NULL). */
+const char *ses3d_gpu_last_error(const ses3d_gpu *h);
+
+/* Model records rhoinv, mu, lambda, A, B, C, Q: compact (nx+1,ny+1,nz+1,5,5,5)
+ * F-order FP32 arrays. Q may be NULL when is_diss == 0. Derives kappa, mu_tau,
+ * cp, cs, rho and the mass matrix.
+ * Replaces SOURCE/ses3d_input.f90:472-501 and SOURCE/ses3d_init.f90:47-61,254-279. */
+int ses3d_gpu_set_model(ses3d_gpu *h, const float *rhoinv, const float *mu, const float *lambda,
+                        const float *A, const float *B, const float *C, const float *Q);
+
+/* Point source of one event, in the event-file units: colatitude and longitude
+ * in degrees, depth in m; source_type 1/2/3 single force, 10 moment tensor with
+ * mom = {Mxx, Myy, Mzz, Mxy, Mxz, Myz}; so = nt source-time-function samples.
+ * Locates the source element and local coordinates as the reference does.
+ * *is_source (may be NULL) receives 1 if the source lies in the box.
+ * Replaces SOURCE/ses3d_input.f90:319-320,405-437 and SOURCE/ses3d_init.f90:363-439
+ * (the per-step injection, SOURCE/ses3d_miscellaneous.f90:11-150, runs on the GPU). */
+int ses3d_gpu_set_source(ses3d_gpu *h, int event, float xxs_deg, float yys_deg, float zzs,
+                         int source_type, const float mom[6], const float *so, int *is_source);
+
+/* Receivers of one event: recloc = nr_global x (colatitude deg, longitude deg,
+ * depth m) as in recfile_<id>. Locates each receiver (last matching element
+ * wins). *nr_out receives the number kept (receivers inside the box);
+ * kept (may be NULL, nr_global entries) receives for each kept receiver, in
+ * order, its 0-based index in recloc.
+ * Replaces SOURCE/ses3d_input.f90:533-544 and SOURCE/ses3d_init.f90:285-357. */
+int ses3d_gpu_set_receivers(ses3d_gpu *h, int event, int nr_global, const float *recloc,
+                            int *nr_out, int *kept);
+
+/* Adjoint sources of one event (adjoint_flag == 2): loc = n x (colat deg, lon
+ * deg, depth m) as in ad_srcfile; stf = n x 3 x nt samples (x, y, z) as in
+ * ad_src_<k>, applied in file order. *n_out receives the number in the box.
+ * Replaces SOURCE/ses3d_input.f90:584-618 and SOURCE/ses3d_init.f90:445-572. */
+int ses3d_gpu_set_adjoint_sources(ses3d_gpu *h, int event, int n, const float *loc,
+                                  const float *stf, int *n_out);
+
+/* Runs n iterations of the time loop body for all events: ses3d_evolution,
+ * record_seismograms (flags 0/1), forward-field store (flag 1) and ses3d_grad
+ * (flag 2). Replaces SOURCE/ses3d_main.f90:95-178 with
+ * SOURCE/ses3d_evolution.f90:7-373, SOURCE/ses3d_output.f90:456-497,
+ * SOURCE/ses3d_main.f90:142-166 and SOURCE/ses3d_grad.f90:25-85. */
+int ses3d_gpu_step(ses3d_gpu *h, int n);
+
+/* Completed iterations (the reference `it` after the last step). */
+int ses3d_gpu_current_step(const ses3d_gpu *h);
+
+/* Velocity seismograms of one event, each (nr, nt) with the receiver index
+ * fastest (seismogram_x(1:nr,1:nt), SOURCE/ses3d_modules.f90:196-198). Entry
+ * it-1 holds the value recorded in iteration it (the pre-update velocity). */
+int ses3d_gpu_get_seismograms(ses3d_gpu *h, int event, float *sx, float *sy, float *sz);
+
+/* Field identifiers for ses3d_gpu_get_field. */
+enum {
+  SES3D_FIELD_VX = 0, SES3D_FIELD_VY, SES3D_FIELD_VZ, /* local form of the current global v */
+  SES3D_FIELD_VX_GLOBAL, SES3D_FIELD_VY_GLOBAL, SES3D_FIELD_VZ_GLOBAL, /* assembled v */
+  SES3D_FIELD_SXX_PML, SES3D_FIELD_SYY_PML, SES3D_FIELD_SZZ_PML, SES3D_FIELD_SXY_PML,
+  SES3D_FIELD_SYX_PML, SES3D_FIELD_SXZ_PML, SES3D_FIELD_SZX_PML, SES3D_FIELD_SYZ_PML,
+  SES3D_FIELD_SZY_PML,
+  SES3D_FIELD_DXUX, SES3D_FIELD_DYUY, SES3D_FIELD_DZUZ, SES3D_FIELD_DXUY, SES3D_FIELD_DYUX,
+  SES3D_FIELD_DXUZ, SES3D_FIELD_DZUX, SES3D_FIELD_DYUZ, SES3D_FIELD_DZUY,
+  SES3D_FIELD_MXX, SES3D_FIELD_MYY, SES3D_FIELD_MZZ, SES3D_FIELD_MXY, SES3D_FIELD_MXZ,
+  SES3D_FIELD_MYZ, /* memory variables: (3, nx+1, ..., 5) mechanism fastest */
+  SES3D_FIELD_MM_GLOBAL, /* assembled mass matrix */
+  SES3D_FIELD_COUNT
+};
+
+/* One field of one event in the reference layout (local fields: N = 125(nx+1)(ny+1)(nz+1)
+ * floats; memory variables 3N; global fields ((nx+1)*4+1)((ny+1)*4+1)((nz+1)*4+1)).
+ * SES3D_FIELD_VX..VZ are the snapshot fields of ses3d_output (SOURCE/ses3d_output.f90:293-312). */
+int ses3d_gpu_get_field(ses3d_gpu *h, int event, int field, float *out);
+
+/* Sets one state field (same layout as get_field) -- restart / test injection. */
+int ses3d_gpu_set_field(ses3d_gpu *h, int event, int field, const float *in);
+
+/* Kernel identifiers for ses3d_gpu_get_kernel. */
+enum {
+  SES3D_KERNEL_RHO = 0, SES3D_KERNEL_CP, SES3D_KERNEL_CSH, SES3D_KERNEL_CSV,
+  SES3D_KERNEL_Q_MU, SES3D_KERNEL_ALPHA_MU, SES3D_KERNEL_Q_KAPPA, SES3D_KERNEL_ALPHA_KAPPA,
+  SES3D_KERNEL_COUNT
+};
+
+/* Frechet kernel of one event (FP64 accumulator) in the reference layout, N doubles:
+ * grad_rho, grad_cp, grad_csh, grad_csv (SOURCE/ses3d_output.f90:318-342) and the
+ * research Q kernels of SOURCE/ses3d_grad_Q.f90 (normalised after the last step). */
+int ses3d_gpu_get_kernel(ses3d_gpu *h, int event, int which, double *out);
+
+/* Forward-field records kept in device memory by an adjoint_flag == 1 run: one
+ * record per stored iteration (it == 1, it % samp_ad == 0, it == nt), 9 fields of
+ * N floats each: vx, vy, vz, exx, eyy, ezz, exy, exz, eyz -- the fields and order of
+ * the ffd/<name>_<rank> files (SOURCE/ses3d_main.f90:148-158, SOURCE/ses3d_output.f90:138-162). */
+int ses3d_gpu_record_count(const ses3d_gpu *h, int event);
+int ses3d_gpu_get_record(ses3d_gpu *h, int event, int record, float *out);
+int ses3d_gpu_put_record(ses3d_gpu *h, int event, int record, const float *in);
+
+/* saving_vector of the forward run (nt entries; it where stored, else 0);
+ * SOURCE/ses3d_main.f90:162 and SOURCE/ses3d_output.f90:379-392. */
+int ses3d_gpu_get_saving_vector(const ses3d_gpu *h, int *out);
+int ses3d_gpu_set_saving_vector(ses3d_gpu *h, const int *in);
+
+/* Switches a handle that completed a flag-1 forward run into the flag-2 adjoint
+ * run over the same records: zeroes the wavefield, keeps model, records and
+ * saving_vector, sets it = 0 (the reference runs this as a second program start). */
+int ses3d_gpu_begin_adjoint(ses3d_gpu *h);
+
+/* Setup quantities for bit-exact checks of the index work of ses3d_init.
+ * Integers: "nr", "rx", "ry", "rz", "isx", "isy", "isz", "is_source", "nr_adsrc", "is"
+ * (3 x nr_adsrc); reals: "recloc_std" (3 x nr), "xxs_loc", "yys_loc", "zzs_loc",
+ * "x", "y", "z" (element-node coordinates), "dl", "knots", "w", "Jac", "dx", "dy", "dz",
+ * "prof_x", "prof_y", "prof_z", "taper" (N, reference layout). Returns the count
+ * written (out may be NULL to query the size) or a negative code. */
+long ses3d_gpu_get_setup_int(ses3d_gpu *h, int event, const char *name, int *out);
+long ses3d_gpu_get_setup_real(ses3d_gpu *h, int event, const char *name, float *out);
+
+/* Non-finite watchdog: the max |v| of each event at the last step (the quantity the
+ * reference prints every step, SOURCE/ses3d_main.f90:111-130). */
+int ses3d_gpu_vmax(ses3d_gpu *h, float *out);
+
+/* Device-resident interface (zero-copy for PyTorch / CUDA callers). Pointers are
+ * device pointers on the handle's device; layouts are the reference layouts.
+ * Model upload from device memory: */
+int ses3d_gpu_set_model_device(ses3d_gpu *h, const float *rhoinv, const float *mu,
+                               const float *lambda, const float *A, const float *B,
+                               const float *C, const float *Q);
+
+/* The CUDA stream the handle launches on (cudaStream_t as void*). */
+void *ses3d_gpu_stream(ses3d_gpu *h);
+
+/* Timing/diagnostic counters: kernel launches issued by the library since create. */
+int64_t ses3d_gpu_launch_count(const ses3d_gpu *h);
+
+/* Captures the launch sequence of `n_per_graph` plain forward iterations into a
+ * CUDA graph and replays it for subsequent ses3d_gpu_step calls (adjoint_flag 0
+ * only; stored/gradient iterations always run eagerly). enable = 0 disables it. */
+int ses3d_gpu_use_graph(ses3d_gpu *h, int enable, int n_per_graph);
+
+/* Per-kernel device time: with profiling enabled, each eager iteration records CUDA
+ * events on the handle's stream around its launches; which = 0 k_element, 1 k_node,
+ * 2 k_receivers, 3 k_inject. ses3d_gpu_profile(h, 1) also resets the totals. */
+int ses3d_gpu_profile(ses3d_gpu *h, int enable);
+int ses3d_gpu_kernel_time(const ses3d_gpu *h, int which, double *total_ms, int64_t *launches);
+
+/* Element-kernel block shape: elements per CTA (1, 2 or 4); 0 selects the default.
+ * bench.py's autotuner sets it. */
+int ses3d_gpu_set_block_elements(ses3d_gpu *h, int elements_per_cta);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SES3D_GPU_H */

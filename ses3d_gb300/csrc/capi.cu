@@ -1,0 +1,1025 @@
+// capi.cu -- implementation of the C ABI declared in include/ses3d_gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/ses3d_gpu.h"
+#include "kernels.cuh"
+#include "setup.hpp"
+
+namespace ses3d {
+cudaError_t launch_element(int diss, int mode, int epb, const Consts &c, const Ptrs &p, cudaStream_t st);
+cudaError_t launch_node(const Consts &c, const Ptrs &p, cudaStream_t st);
+cudaError_t launch_receivers(const Consts &c, const float *v, const int *rec_elem, const int *rec_ev,
+                             const float *rec_w, float *seis, int R, const int *d_it, cudaStream_t st);
+cudaError_t launch_inject(const Consts &c, float *f, const int4 *groups, int ngroups, const float *delta,
+                          const float *stf, const int *mask, const int *d_it, cudaStream_t st);
+cudaError_t launch_transpose(const float *in, float *out, long long rows, long long cols, cudaStream_t st);
+cudaError_t launch_transpose_d(const double *in, double *out, long long rows, long long cols, cudaStream_t st);
+cudaError_t launch_derive(const float *raw, float *mat, float *gm, long long N, int is_diss, float sum_D_p,
+                          cudaStream_t st);
+cudaError_t launch_mass(const Consts &c, const float *rhoinv, const float *z, const float *sinx, const float *w,
+                        float Jac, float *MM, cudaStream_t st);
+cudaError_t launch_vmax(const float *v, long long G3, int nev, unsigned int *out, cudaStream_t st);
+cudaError_t launch_grad_q_norm(const Consts &c, const float *gm, double *grad, cudaStream_t st);
+cudaError_t launch_gather_ref(const Consts &c, const float *v, float *out, cudaStream_t st);
+}  // namespace ses3d
+
+using namespace ses3d;
+
+namespace {
+thread_local std::string g_create_error;
+
+struct EventHost {
+  int source_type = 0;
+  PointSource src;
+  std::vector<float> so;
+  std::vector<Receiver> recs;
+  std::vector<AdjointSource> adj;
+  std::vector<float> adj_stf;  // [n_local][3][nt]
+};
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+}  // namespace
+
+struct ses3d_gpu {
+  ses3d_config cfg;
+  Geometry geo;
+  int device = 0;
+  cudaStream_t st = nullptr;
+  std::string err;
+  int it = 0;
+  int mode_flag = 0;  // current adjoint_flag
+  bool model_set = false;
+  int epb = 1;
+  long long launches = 0;
+  Consts c;
+  // device memory
+  KTab *d_ktab = nullptr;
+  float *d_tab = nullptr;  // sin_x | cot_x | r_z | pxr | pyr | pzr | pxg | pyg | pzg | z | w
+  float *d_MM = nullptr, *d_mat = nullptr, *d_gmat = nullptr;
+  float *d_state = nullptr, *d_v = nullptr, *d_f = nullptr;
+  int *d_it = nullptr;
+  int *d_src_elem = nullptr;
+  float *d_src_delta = nullptr, *d_src_mom = nullptr, *d_stf = nullptr;
+  int4 *d_groups = nullptr;
+  float *d_fdelta = nullptr, *d_fstf = nullptr;
+  int *d_fmask = nullptr;
+  int ngroups = 0;
+  int R = 0;
+  int *d_rec_elem = nullptr, *d_rec_ev = nullptr;
+  float *d_rec_w = nullptr, *d_seis = nullptr;
+  std::vector<int> rec_off;  // [nev+1]
+  double *d_grad = nullptr;
+  unsigned int *d_scratch_u = nullptr;
+  std::vector<float *> records;  // each [nev][NREC][N]
+  int record_cursor = 0;
+  std::vector<int> saving_vector;  // [nt+1]
+  std::vector<EventHost> ev;
+  // tables offsets
+  size_t o_sin = 0, o_cot = 0, o_r = 0, o_pxr = 0, o_pyr = 0, o_pzr = 0, o_pxg = 0, o_pyg = 0, o_pzg = 0, o_z = 0,
+         o_w = 0;
+  // per-kernel timing
+  bool prof_on = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+  double prof_ms[4] = {0, 0, 0, 0};
+  long long prof_n[4] = {0, 0, 0, 0};
+  // graph
+  bool graph_on = false;
+  int graph_n = 0;
+  cudaGraphExec_t graph_exec = nullptr;
+  bool graph_dirty = true;
+};
+
+namespace {
+
+int fail(ses3d_gpu *h, int code, const std::string &msg) {
+  if (h) h->err = msg; else g_create_error = msg;
+  return code;
+}
+
+int cuda_fail(ses3d_gpu *h, cudaError_t e, const char *where) {
+  std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+  return fail(h, SES3D_E_CUDA, m);
+}
+
+#define CK(h, call)                                              \
+  do {                                                           \
+    cudaError_t _e = (call);                                     \
+    if (_e != cudaSuccess) return cuda_fail((h), _e, #call);     \
+  } while (0)
+
+template <class T> cudaError_t dalloc(T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMalloc((void **)p, count * sizeof(T));
+}
+
+void dfree(void *p) {
+  if (p) cudaFree(p);
+}
+
+Ptrs make_ptrs(ses3d_gpu *h) {
+  Ptrs p;
+  std::memset(&p, 0, sizeof(p));
+  p.ktab = h->d_ktab;
+  p.sin_x = h->d_tab + h->o_sin; p.cot_x = h->d_tab + h->o_cot; p.r_z = h->d_tab + h->o_r;
+  p.pxr = h->d_tab + h->o_pxr; p.pyr = h->d_tab + h->o_pyr; p.pzr = h->d_tab + h->o_pzr;
+  p.pxg = h->d_tab + h->o_pxg; p.pyg = h->d_tab + h->o_pyg; p.pzg = h->d_tab + h->o_pzg;
+  p.MM = h->d_MM; p.mat = h->d_mat; p.gmat = h->d_gmat;
+  p.state = h->d_state; p.v = h->d_v; p.f = h->d_f; p.d_it = h->d_it;
+  p.src_elem = h->d_src_elem; p.src_delta = h->d_src_delta; p.src_mom = h->d_src_mom; p.stf = h->d_stf;
+  p.grad = h->d_grad;
+  p.grad_q = h->cfg.grad_variant == 1;
+  return p;
+}
+
+void destroy_graph(ses3d_gpu *h) {
+  if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+  h->graph_exec = nullptr;
+  h->graph_dirty = true;
+}
+
+// Rebuild the point-force groups (single forces and adjoint sources) of all events.
+int rebuild_forces(ses3d_gpu *h) {
+  const int nt = h->cfg.nt;
+  std::map<std::pair<int, long long>, std::vector<int>> groups;  // (event, element) -> sources
+  std::vector<float> delta, stf;
+  std::vector<int> mask;
+  int ns = 0;
+  for (int e = 0; e < h->cfg.n_events; ++e) {
+    const EventHost &E = h->ev[e];
+    const Geometry &g = h->geo;
+    if (h->mode_flag <= 1 && E.src.is_source && E.source_type >= 1 && E.source_type <= 3) {
+      long long el = E.src.isx + (long long)g.ex * (E.src.isy + (long long)g.ey * E.src.isz);
+      groups[{e, el}].push_back(ns++);
+      delta.insert(delta.end(), E.src.delta, E.src.delta + NPE);
+      for (int cc = 0; cc < 3; ++cc) {
+        if (cc == E.source_type - 1) stf.insert(stf.end(), E.so.begin(), E.so.end());
+        else stf.insert(stf.end(), (size_t)nt, 0.f);
+      }
+      mask.push_back(1 << (E.source_type - 1));
+    }
+    if (h->mode_flag == 2) {
+      for (size_t s = 0; s < E.adj.size(); ++s) {
+        const AdjointSource &A = E.adj[s];
+        long long el = A.is[0] + (long long)g.ex * (A.is[1] + (long long)g.ey * A.is[2]);
+        groups[{e, el}].push_back(ns++);
+        delta.insert(delta.end(), A.delta, A.delta + NPE);
+        stf.insert(stf.end(), E.adj_stf.begin() + s * 3 * nt, E.adj_stf.begin() + (s + 1) * 3 * nt);
+        mask.push_back(7);
+      }
+    }
+  }
+  // flatten: sources of a group contiguous, in file order
+  std::vector<int4> gr;
+  std::vector<float> d2, s2;
+  std::vector<int> m2;
+  int k = 0;
+  for (auto &kv : groups) {
+    int4 g4;
+    g4.x = kv.first.first; g4.y = (int)kv.first.second; g4.z = k;
+    for (int s : kv.second) {
+      d2.insert(d2.end(), delta.begin() + (size_t)s * NPE, delta.begin() + (size_t)(s + 1) * NPE);
+      s2.insert(s2.end(), stf.begin() + (size_t)s * 3 * nt, stf.begin() + (size_t)(s + 1) * 3 * nt);
+      m2.push_back(mask[s]);
+      ++k;
+    }
+    g4.w = k;
+    gr.push_back(g4);
+  }
+  dfree(h->d_groups); dfree(h->d_fdelta); dfree(h->d_fstf); dfree(h->d_fmask);
+  h->d_groups = nullptr; h->d_fdelta = nullptr; h->d_fstf = nullptr; h->d_fmask = nullptr;
+  h->ngroups = (int)gr.size();
+  if (h->ngroups) {
+    CK(h, dalloc(&h->d_groups, gr.size()));
+    CK(h, dalloc(&h->d_fdelta, d2.size()));
+    CK(h, dalloc(&h->d_fstf, s2.size()));
+    CK(h, dalloc(&h->d_fmask, m2.size()));
+    CK(h, cudaMemcpy(h->d_groups, gr.data(), gr.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->d_fdelta, d2.data(), d2.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->d_fstf, s2.data(), s2.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->d_fmask, m2.data(), m2.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  destroy_graph(h);
+  return SES3D_OK;
+}
+
+int upload_moment_sources(ses3d_gpu *h) {
+  const int nev = h->cfg.n_events, nt = h->cfg.nt;
+  std::vector<int> el(nev, -1);
+  std::vector<float> delta((size_t)nev * NPE, 0.f), stf((size_t)nev * nt, 0.f);
+  for (int e = 0; e < nev; ++e) {
+    const EventHost &E = h->ev[e];
+    if (h->mode_flag <= 1 && E.src.is_source && E.source_type == 10) {
+      el[e] = E.src.isx + h->geo.ex * (E.src.isy + h->geo.ey * E.src.isz);
+      std::memcpy(&delta[(size_t)e * NPE], E.src.delta, NPE * sizeof(float));
+    }
+    if (!E.so.empty()) std::memcpy(&stf[(size_t)e * nt], E.so.data(), nt * sizeof(float));
+  }
+  CK(h, cudaMemcpy(h->d_src_elem, el.data(), nev * sizeof(int), cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->d_src_delta, delta.data(), delta.size() * sizeof(float), cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->d_stf, stf.data(), stf.size() * sizeof(float), cudaMemcpyHostToDevice));
+  destroy_graph(h);
+  return SES3D_OK;
+}
+
+// Transpose of an N-sized field: internal (E x 125) -> reference (125 x E).
+int to_ref(ses3d_gpu *h, const float *d_int, float *d_ref) {
+  CK(h, launch_transpose(d_int, d_ref, h->geo.E, NPE, h->st));
+  return SES3D_OK;
+}
+int from_ref(ses3d_gpu *h, const float *d_ref, float *d_int) {
+  CK(h, launch_transpose(d_ref, d_int, NPE, h->geo.E, h->st));
+  return SES3D_OK;
+}
+
+int check_event(ses3d_gpu *h, int event) {
+  if (!h) return SES3D_E_CONFIG;
+  if (event < 0 || event >= h->cfg.n_events) return fail(h, SES3D_E_CONFIG, "event index out of range");
+  return SES3D_OK;
+}
+
+int set_model_common(ses3d_gpu *h, float *d_raw) {
+  const long long N = h->geo.N;
+  float *d_tmp = nullptr;
+  CK(h, dalloc(&d_tmp, (size_t)(NMAT + NGMAT) * N));
+  float sum_D_p = h->cfg.D_p[0];
+  sum_D_p = sum_D_p + h->cfg.D_p[1];
+  sum_D_p = sum_D_p + h->cfg.D_p[2];
+  cudaError_t e = launch_derive(d_raw, d_tmp, d_tmp + (size_t)NMAT * N, N, h->cfg.is_diss, sum_D_p, h->st);
+  if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "derive"); }
+  for (int f = 0; f < NMAT; ++f) {
+    e = launch_transpose(d_tmp + (size_t)f * N, h->d_mat + (size_t)f * N, NPE, h->geo.E, h->st);
+    if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "transpose mat"); }
+  }
+  for (int f = 0; f < NGMAT; ++f) {
+    e = launch_transpose(d_tmp + (size_t)(NMAT + f) * N, h->d_gmat + (size_t)f * N, NPE, h->geo.E, h->st);
+    if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "transpose gmat"); }
+  }
+  e = launch_mass(h->c, d_raw, h->d_tab + h->o_z, h->d_tab + h->o_sin, h->d_tab + h->o_w, h->geo.Jac, h->d_MM, h->st);
+  if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "mass"); }
+  h->launches += 2 + NMAT + NGMAT;
+  e = cudaStreamSynchronize(h->st);
+  dfree(d_tmp);
+  if (e != cudaSuccess) return cuda_fail(h, e, "set_model");
+  h->model_set = true;
+  return SES3D_OK;
+}
+
+int zero_wavefield(ses3d_gpu *h) {
+  const size_t nev = h->cfg.n_events;
+  CK(h, cudaMemsetAsync(h->d_state, 0, nev * NSTATE * h->geo.N * sizeof(float), h->st));
+  CK(h, cudaMemsetAsync(h->d_v, 0, nev * 3 * h->geo.G * sizeof(float), h->st));
+  CK(h, cudaMemsetAsync(h->d_f, 0, nev * 3 * h->geo.N * sizeof(float), h->st));
+  CK(h, cudaMemsetAsync(h->d_it, 0, sizeof(int), h->st));
+  if (h->d_seis) CK(h, cudaMemsetAsync(h->d_seis, 0, (size_t)3 * h->cfg.nt * h->R * sizeof(float), h->st));
+  h->it = 0;
+  return SES3D_OK;
+}
+
+cudaEvent_t pool_event(ses3d_gpu *h) {
+  if (!h->ev_pool.empty()) {
+    cudaEvent_t e = h->ev_pool.back();
+    h->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Adds the durations of completed timed launches (the stream has been synchronised).
+void collect_times(ses3d_gpu *h) {
+  for (auto &pe : h->ev_pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, pe.second.first, pe.second.second) == cudaSuccess) {
+      h->prof_ms[pe.first] += ms;
+      h->prof_n[pe.first] += 1;
+    }
+    h->ev_pool.push_back(pe.second.first);
+    h->ev_pool.push_back(pe.second.second);
+  }
+  h->ev_pending.clear();
+}
+
+struct Timed {
+  ses3d_gpu *h;
+  int which;
+  cudaEvent_t a = nullptr, b = nullptr;
+  Timed(ses3d_gpu *h_, int w, bool on) : h(h_), which(w) {
+    if (on) { a = pool_event(h); b = pool_event(h); cudaEventRecord(a, h->st); }
+  }
+  ~Timed() {
+    if (a) { cudaEventRecord(b, h->st); h->ev_pending.push_back({which, {a, b}}); }
+  }
+};
+
+// one iteration: receivers, element, inject, node (+ record / kernel work)
+int launch_iteration(ses3d_gpu *h, int mode, float *rec, bool timed = false) {
+  Ptrs p = make_ptrs(h);
+  p.rec = rec;
+  const int flag = h->mode_flag;
+  if ((flag == 0 || flag == 1) && h->R > 0) {
+    Timed t(h, 2, timed);
+    CK(h, launch_receivers(h->c, h->d_v, h->d_rec_elem, h->d_rec_ev, h->d_rec_w, h->d_seis, h->R, h->d_it, h->st));
+    ++h->launches;
+  }
+  {
+    Timed t(h, 0, timed);
+    CK(h, launch_element(h->cfg.is_diss, mode, h->epb, h->c, p, h->st));
+    ++h->launches;
+  }
+  if (h->ngroups) {
+    Timed t(h, 3, timed);
+    CK(h, launch_inject(h->c, h->d_f, h->d_groups, h->ngroups, h->d_fdelta, h->d_fstf, h->d_fmask, h->d_it, h->st));
+    ++h->launches;
+  }
+  {
+    Timed t(h, 1, timed);
+    CK(h, launch_node(h->c, p, h->st));
+    ++h->launches;
+  }
+  return SES3D_OK;
+}
+
+int build_graph(ses3d_gpu *h) {
+  destroy_graph(h);
+  cudaGraph_t graph;
+  CK(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+  long long before = h->launches;
+  for (int s = 0; s < h->graph_n; ++s) {
+    int rc = launch_iteration(h, 0, nullptr);
+    if (rc) {
+      cudaStreamEndCapture(h->st, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+  }
+  h->launches = before;  // counted at replay
+  CK(h, cudaStreamEndCapture(h->st, &graph));
+  cudaError_t e = cudaGraphInstantiate(&h->graph_exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+  h->graph_dirty = false;
+  return SES3D_OK;
+}
+
+int launches_per_iteration(ses3d_gpu *h) {
+  int n = 2;
+  if ((h->mode_flag == 0 || h->mode_flag == 1) && h->R > 0) ++n;
+  if (h->ngroups) ++n;
+  return n;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *ses3d_gpu_version(void) { return "ses3d_gb300 0.1 (sm_103a)"; }
+
+const char *ses3d_gpu_last_error(const ses3d_gpu *h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
+  if (!cfg || !out) return fail(nullptr, SES3D_E_CONFIG, "null argument");
+  *out = nullptr;
+  if (cfg->lpd != LPD) return fail(nullptr, SES3D_E_CONFIG, "only lpd = 4 is implemented");
+  if (cfg->n_events < 1) return fail(nullptr, SES3D_E_CONFIG, "n_events must be >= 1");
+  if (cfg->nt < 1) return fail(nullptr, SES3D_E_CONFIG, "nt must be >= 1");
+  if (!(cfg->dt > 0.f)) return fail(nullptr, SES3D_E_CONFIG, "dt must be > 0");
+  if (cfg->adjoint_flag < 0 || cfg->adjoint_flag > 2) return fail(nullptr, SES3D_E_CONFIG, "adjoint_flag must be 0, 1 or 2");
+  if (cfg->adjoint_flag >= 1 && cfg->samp_ad < 1) return fail(nullptr, SES3D_E_CONFIG, "samp_ad must be >= 1");
+  if (cfg->is_diss != 0 && cfg->is_diss != 1) return fail(nullptr, SES3D_E_CONFIG, "is_diss must be 0 or 1");
+  if (cfg->is_diss == 1)
+    for (int k = 0; k < 3; ++k)
+      if (!(cfg->tau_p[k] > 0.f)) return fail(nullptr, SES3D_E_CONFIG, "relaxation times must be > 0");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(nullptr, SES3D_E_NODEV, "no CUDA device");
+  ses3d_gpu *h = new ses3d_gpu();
+  h->cfg = *cfg;
+  h->mode_flag = cfg->adjoint_flag;
+  cudaGetDevice(&h->device);
+  std::string msg = build_geometry(h->geo, cfg->nx, cfg->ny, cfg->nz, cfg->pml, cfg->xmin, cfg->xmax, cfg->ymin,
+                                   cfg->ymax, cfg->zmin, cfg->zmax, cfg->zmax_global);
+  if (!msg.empty()) { delete h; return fail(nullptr, SES3D_E_CONFIG, msg); }
+  const Geometry &g = h->geo;
+  if (g.N * (long long)cfg->n_events > (1LL << 40)) { delete h; return fail(nullptr, SES3D_E_CONFIG, "mesh too large"); }
+  // constants
+  Consts &c = h->c;
+  std::memset(&c, 0, sizeof(c));
+  c.ex = g.ex; c.ey = g.ey; c.ez = g.ez; c.nev = cfg->n_events; c.nt = cfg->nt;
+  c.GX = g.GX; c.GY = g.GY; c.GZ = g.GZ; c.E = g.E; c.N = g.N; c.G = g.G;
+  c.dt = cfg->dt;
+  for (int k = 0; k < 3; ++k) {
+    c.tau_p[k] = cfg->tau_p[k]; c.D_p[k] = cfg->D_p[k];
+    if (cfg->is_diss) {
+      c.a_k[k] = cfg->dt / cfg->tau_p[k];
+      c.L_k[k] = cfg->dt * cfg->D_p[k] / cfg->tau_p[k];
+    }
+  }
+  c.s_grad = (float)cfg->samp_ad * cfg->dt;
+  c.Jac = g.Jac;
+  c.inv_jac = 1.f / g.Jac;
+  // coefficient tables
+  KTab kt;
+  for (int i = 0; i < NP; ++i)
+    for (int q = 0; q < NP; ++q) {
+      kt.Dx[i][q] = 2.0f * g.dl[q][i] / g.dx;
+      kt.Dy[i][q] = 2.0f * g.dl[q][i] / g.dy;
+      kt.Dz[i][q] = 2.0f * g.dl[q][i] / g.dz;
+      kt.dlT[i][q] = g.dl[i][q];
+    }
+  for (int a = 0; a < NP; ++a)
+    for (int b = 0; b < NP; ++b) {
+      kt.CX[a][b] = (2.0f / g.dx) * g.Jac * g.w[a] * g.w[b];
+      kt.CY[a][b] = (2.0f / g.dy) * g.Jac * g.w[a] * g.w[b];
+      kt.CZ[a][b] = -((2.0f / g.dz) * g.Jac * g.w[a] * g.w[b]);
+    }
+  for (int n = 0; n < NP; ++n) kt.w[n] = g.w[n];
+  // table block
+  std::vector<float> tab;
+  auto put = [&](size_t &off, const std::vector<float> &v) { off = tab.size(); tab.insert(tab.end(), v.begin(), v.end()); };
+  put(h->o_sin, g.sin_x); put(h->o_cot, g.cot_x); put(h->o_r, g.z);
+  put(h->o_pxr, g.pxr); put(h->o_pyr, g.pyr); put(h->o_pzr, g.pzr);
+  put(h->o_pxg, g.pxg); put(h->o_pyg, g.pyg); put(h->o_pzg, g.pzg);
+  put(h->o_z, g.z);
+  put(h->o_w, std::vector<float>(g.w, g.w + NP));
+  const size_t nev = cfg->n_events;
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t x) { if (x != cudaSuccess && e == cudaSuccess) e = x; };
+  chk(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+  chk(dalloc(&h->d_ktab, 1));
+  chk(dalloc(&h->d_tab, tab.size()));
+  chk(dalloc(&h->d_MM, (size_t)g.G));
+  chk(dalloc(&h->d_mat, (size_t)NMAT * g.N));
+  chk(dalloc(&h->d_gmat, (size_t)NGMAT * g.N));
+  chk(dalloc(&h->d_state, nev * NSTATE * g.N));
+  chk(dalloc(&h->d_v, nev * 3 * g.G));
+  chk(dalloc(&h->d_f, nev * 3 * g.N));
+  chk(dalloc(&h->d_it, 1));
+  chk(dalloc(&h->d_src_elem, nev));
+  chk(dalloc(&h->d_src_delta, nev * NPE));
+  chk(dalloc(&h->d_src_mom, nev * 6));
+  chk(dalloc(&h->d_stf, nev * cfg->nt));
+  chk(dalloc(&h->d_scratch_u, nev));
+  if (cfg->adjoint_flag == 2) chk(dalloc(&h->d_grad, nev * NGRAD * g.N));
+  if (e != cudaSuccess) {
+    std::string m = std::string("allocation: ") + cudaGetErrorString(e);
+    ses3d_gpu_destroy(h);
+    return fail(nullptr, e == cudaErrorMemoryAllocation ? SES3D_E_OOM : SES3D_E_CUDA, m);
+  }
+  chk(cudaMemcpy(h->d_ktab, &kt, sizeof(KTab), cudaMemcpyHostToDevice));
+  chk(cudaMemcpy(h->d_tab, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice));
+  std::vector<int> minus1(nev, -1);
+  chk(cudaMemcpy(h->d_src_elem, minus1.data(), nev * sizeof(int), cudaMemcpyHostToDevice));
+  chk(cudaMemset(h->d_src_delta, 0, nev * NPE * sizeof(float)));
+  chk(cudaMemset(h->d_src_mom, 0, nev * 6 * sizeof(float)));
+  chk(cudaMemset(h->d_stf, 0, nev * cfg->nt * sizeof(float)));
+  chk(cudaMemset(h->d_MM, 0, (size_t)g.G * sizeof(float)));
+  if (h->d_grad) chk(cudaMemset(h->d_grad, 0, nev * NGRAD * g.N * sizeof(double)));
+  if (e != cudaSuccess) {
+    std::string m = std::string("initialisation: ") + cudaGetErrorString(e);
+    ses3d_gpu_destroy(h);
+    return fail(nullptr, SES3D_E_CUDA, m);
+  }
+  h->ev.resize(nev);
+  h->rec_off.assign(nev + 1, 0);
+  h->saving_vector.assign(cfg->nt + 2, 0);
+  int rc = zero_wavefield(h);
+  if (rc) { std::string m = h->err; ses3d_gpu_destroy(h); return fail(nullptr, rc, m); }
+  cudaStreamSynchronize(h->st);
+  *out = h;
+  return SES3D_OK;
+}
+
+int ses3d_gpu_destroy(ses3d_gpu *h) {
+  if (!h) return SES3D_OK;
+  if (h->st) cudaStreamSynchronize(h->st);
+  destroy_graph(h);
+  for (auto &pe : h->ev_pending) { h->ev_pool.push_back(pe.second.first); h->ev_pool.push_back(pe.second.second); }
+  for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  void *ptrs[] = {h->d_ktab, h->d_tab, h->d_MM, h->d_mat, h->d_gmat, h->d_state, h->d_v, h->d_f, h->d_it,
+                  h->d_src_elem, h->d_src_delta, h->d_src_mom, h->d_stf, h->d_groups, h->d_fdelta, h->d_fstf,
+                  h->d_fmask, h->d_rec_elem, h->d_rec_ev, h->d_rec_w, h->d_seis, h->d_grad, h->d_scratch_u};
+  for (void *p : ptrs) dfree(p);
+  for (float *r : h->records) dfree(r);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return SES3D_OK;
+}
+
+int ses3d_gpu_set_model(ses3d_gpu *h, const float *rhoinv, const float *mu, const float *lambda, const float *A,
+                        const float *B, const float *C, const float *Q) {
+  if (!h) return SES3D_E_CONFIG;
+  if (!rhoinv || !mu || !lambda || !A || !B || !C) return fail(h, SES3D_E_CONFIG, "null model array");
+  if (h->cfg.is_diss && !Q) return fail(h, SES3D_E_CONFIG, "Q is required when is_diss = 1");
+  const long long N = h->geo.N;
+  float *d_raw = nullptr;
+  CK(h, dalloc(&d_raw, (size_t)7 * N));
+  const float *src[7] = {rhoinv, mu, lambda, A, B, C, Q};
+  for (int k = 0; k < 7; ++k) {
+    if (!src[k]) continue;
+    cudaError_t e = cudaMemcpyAsync(d_raw + (size_t)k * N, src[k], N * sizeof(float), cudaMemcpyHostToDevice, h->st);
+    if (e != cudaSuccess) { dfree(d_raw); return cuda_fail(h, e, "set_model copy"); }
+  }
+  int rc = set_model_common(h, d_raw);
+  dfree(d_raw);
+  return rc;
+}
+
+int ses3d_gpu_set_model_device(ses3d_gpu *h, const float *rhoinv, const float *mu, const float *lambda,
+                               const float *A, const float *B, const float *C, const float *Q) {
+  if (!h) return SES3D_E_CONFIG;
+  if (!rhoinv || !mu || !lambda || !A || !B || !C) return fail(h, SES3D_E_CONFIG, "null model array");
+  if (h->cfg.is_diss && !Q) return fail(h, SES3D_E_CONFIG, "Q is required when is_diss = 1");
+  const long long N = h->geo.N;
+  float *d_raw = nullptr;
+  CK(h, dalloc(&d_raw, (size_t)7 * N));
+  const float *src[7] = {rhoinv, mu, lambda, A, B, C, Q};
+  for (int k = 0; k < 7; ++k) {
+    if (!src[k]) continue;
+    cudaError_t e = cudaMemcpyAsync(d_raw + (size_t)k * N, src[k], N * sizeof(float), cudaMemcpyDeviceToDevice, h->st);
+    if (e != cudaSuccess) { dfree(d_raw); return cuda_fail(h, e, "set_model_device copy"); }
+  }
+  int rc = set_model_common(h, d_raw);
+  dfree(d_raw);
+  return rc;
+}
+
+int ses3d_gpu_set_source(ses3d_gpu *h, int event, float xxs_deg, float yys_deg, float zzs, int source_type,
+                         const float mom[6], const float *so, int *is_source) {
+  int rc = check_event(h, event);
+  if (rc) return rc;
+  if (!so) return fail(h, SES3D_E_CONFIG, "null stf");
+  if (source_type == 10 && !mom) return fail(h, SES3D_E_CONFIG, "null moment tensor");
+  EventHost &E = h->ev[event];
+  E.source_type = source_type;
+  locate_source(h->geo, xxs_deg, yys_deg, zzs, source_type, E.src);
+  E.so.assign(so, so + h->cfg.nt);
+  if (is_source) *is_source = E.src.is_source;
+  rc = upload_moment_sources(h);
+  if (rc) return rc;
+  if (source_type == 10) {
+    float m6[6];
+    for (int q = 0; q < 6; ++q) m6[q] = mom[q];
+    CK(h, cudaMemcpy(h->d_src_mom + (size_t)event * 6, m6, 6 * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  return rebuild_forces(h);
+}
+
+int ses3d_gpu_set_receivers(ses3d_gpu *h, int event, int nr_global, const float *recloc, int *nr_out, int *kept) {
+  int rc = check_event(h, event);
+  if (rc) return rc;
+  if (nr_global < 0 || (nr_global > 0 && !recloc)) return fail(h, SES3D_E_CONFIG, "bad receiver list");
+  EventHost &E = h->ev[event];
+  E.recs = locate_receivers(h->geo, nr_global, recloc);
+  if (nr_out) *nr_out = (int)E.recs.size();
+  if (kept)
+    for (size_t r = 0; r < E.recs.size(); ++r) kept[r] = E.recs[r].global_index;
+  // rebuild the receiver table of all events
+  const int nev = h->cfg.n_events;
+  std::vector<int> el, evi;
+  std::vector<float> w;
+  h->rec_off.assign(nev + 1, 0);
+  for (int e = 0; e < nev; ++e) {
+    h->rec_off[e] = (int)el.size();
+    for (const Receiver &r : h->ev[e].recs) {
+      el.push_back(r.rx + h->geo.ex * (r.ry + h->geo.ey * r.rz));
+      evi.push_back(e);
+      w.insert(w.end(), r.weight, r.weight + NPE);
+    }
+  }
+  h->rec_off[nev] = (int)el.size();
+  dfree(h->d_rec_elem); dfree(h->d_rec_ev); dfree(h->d_rec_w); dfree(h->d_seis);
+  h->d_rec_elem = nullptr; h->d_rec_ev = nullptr; h->d_rec_w = nullptr; h->d_seis = nullptr;
+  h->R = (int)el.size();
+  if (h->R) {
+    CK(h, dalloc(&h->d_rec_elem, el.size()));
+    CK(h, dalloc(&h->d_rec_ev, evi.size()));
+    CK(h, dalloc(&h->d_rec_w, w.size()));
+    CK(h, dalloc(&h->d_seis, (size_t)3 * h->cfg.nt * h->R));
+    CK(h, cudaMemcpy(h->d_rec_elem, el.data(), el.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->d_rec_ev, evi.data(), evi.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->d_rec_w, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(h, cudaMemset(h->d_seis, 0, (size_t)3 * h->cfg.nt * h->R * sizeof(float)));
+  }
+  destroy_graph(h);
+  return SES3D_OK;
+}
+
+int ses3d_gpu_set_adjoint_sources(ses3d_gpu *h, int event, int n, const float *loc, const float *stf, int *n_out) {
+  int rc = check_event(h, event);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!loc || !stf))) return fail(h, SES3D_E_CONFIG, "bad adjoint source list");
+  EventHost &E = h->ev[event];
+  E.adj = locate_adjoint_sources(h->geo, n, loc);
+  const int nt = h->cfg.nt;
+  E.adj_stf.clear();
+  for (const AdjointSource &a : E.adj)
+    E.adj_stf.insert(E.adj_stf.end(), stf + (size_t)a.global_index * 3 * nt, stf + (size_t)(a.global_index + 1) * 3 * nt);
+  if (n_out) *n_out = (int)E.adj.size();
+  return rebuild_forces(h);
+}
+
+int ses3d_gpu_step(ses3d_gpu *h, int n) {
+  if (!h) return SES3D_E_CONFIG;
+  if (!h->model_set) return fail(h, SES3D_E_STATE, "set_model must be called before step");
+  if (n < 0) return fail(h, SES3D_E_CONFIG, "n must be >= 0");
+  const int nt = h->cfg.nt;
+  int done = 0;
+  while (done < n && h->it < nt) {
+    const int it = h->it + 1;
+    const int flag = h->mode_flag;
+    if (flag == 0 && h->graph_on && h->graph_n > 0 && n - done >= h->graph_n && nt - h->it >= h->graph_n) {
+      if (h->graph_dirty || !h->graph_exec) {
+        int rc = build_graph(h);
+        if (rc) return rc;
+      }
+      CK(h, cudaGraphLaunch(h->graph_exec, h->st));
+      h->launches += (long long)h->graph_n * launches_per_iteration(h);
+      h->it += h->graph_n;
+      done += h->graph_n;
+      continue;
+    }
+    int mode = 0;
+    float *rec = nullptr;
+    if (flag == 1 && (it % h->cfg.samp_ad == 0 || it == 1 || it == nt)) {
+      CK(h, dalloc(&rec, (size_t)h->cfg.n_events * NREC * h->geo.N));
+      h->records.push_back(rec);
+      h->saving_vector[it] = it;
+      mode = 1;
+    } else if (flag == 2 && h->saving_vector[nt + 1 - it] > 0 && h->record_cursor > 0) {
+      rec = h->records[--h->record_cursor];
+      mode = 2;
+    }
+    int rc = launch_iteration(h, mode, rec, h->prof_on);
+    if (rc) return rc;
+    h->it = it;
+    ++done;
+    if (flag == 2 && h->cfg.grad_variant == 1 && it == nt && h->cfg.is_diss == 1) {
+      CK(h, launch_grad_q_norm(h->c, h->d_gmat, h->d_grad, h->st));
+      ++h->launches;
+    }
+  }
+  CK(h, cudaStreamSynchronize(h->st));
+  collect_times(h);
+  return SES3D_OK;
+}
+
+int ses3d_gpu_current_step(const ses3d_gpu *h) { return h ? h->it : SES3D_E_CONFIG; }
+
+int ses3d_gpu_get_seismograms(ses3d_gpu *h, int event, float *sx, float *sy, float *sz) {
+  int rc = check_event(h, event);
+  if (rc) return rc;
+  const int nr = h->rec_off[event + 1] - h->rec_off[event];
+  if (nr == 0) return SES3D_OK;
+  float *out[3] = {sx, sy, sz};
+  for (int c = 0; c < 3; ++c) {
+    if (!out[c]) continue;
+    CK(h, cudaMemcpy2DAsync(out[c], nr * sizeof(float), h->d_seis + (size_t)c * h->cfg.nt * h->R + h->rec_off[event],
+                            h->R * sizeof(float), nr * sizeof(float), h->cfg.nt, cudaMemcpyDeviceToHost, h->st));
+  }
+  CK(h, cudaStreamSynchronize(h->st));
+  return SES3D_OK;
+}
+
+static int state_field_index(int field) {
+  static const int map[] = {F_SXX, F_SYY, F_SZZ, F_SXY, F_SYX, F_SXZ, F_SZX, F_SYZ, F_SZY,
+                            F_DXUX, F_DYUY, F_DZUZ, F_DXUY, F_DYUX, F_DXUZ, F_DZUX, F_DYUZ, F_DZUY};
+  if (field >= SES3D_FIELD_SXX_PML && field <= SES3D_FIELD_DZUY) return map[field - SES3D_FIELD_SXX_PML];
+  return -1;
+}
+
+static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float *hin) {
+  int rc = check_event(h, event);
+  if (rc) return rc;
+  const long long N = h->geo.N, G = h->geo.G;
+  float *vbase = h->d_v + (size_t)event * 3 * G;
+  float *sbase = h->d_state + (size_t)event * NSTATE * N;
+  if (field >= SES3D_FIELD_VX_GLOBAL && field <= SES3D_FIELD_VZ_GLOBAL) {
+    float *d = vbase + (size_t)(field - SES3D_FIELD_VX_GLOBAL) * G;
+    if (hout) CK(h, cudaMemcpy(hout, d, G * sizeof(float), cudaMemcpyDeviceToHost));
+    else CK(h, cudaMemcpy(d, hin, G * sizeof(float), cudaMemcpyHostToDevice));
+    destroy_graph(h);
+    return SES3D_OK;
+  }
+  if (field == SES3D_FIELD_MM_GLOBAL) {
+    if (!hout) return fail(h, SES3D_E_CONFIG, "MM_global is read-only");
+    CK(h, cudaMemcpy(hout, h->d_MM, G * sizeof(float), cudaMemcpyDeviceToHost));
+    return SES3D_OK;
+  }
+  float *tmp = nullptr, *tmp2 = nullptr;
+  CK(h, dalloc(&tmp, (size_t)N));
+  CK(h, dalloc(&tmp2, (size_t)N));
+  int out_rc = SES3D_OK;
+  auto done = [&](int r) { dfree(tmp); dfree(tmp2); return r; };
+  if (field >= SES3D_FIELD_VX && field <= SES3D_FIELD_VZ) {
+    if (!hout) return done(fail(h, SES3D_E_CONFIG, "local v is derived from the global v; set the global field"));
+    Consts c1 = h->c;
+    cudaError_t e = launch_gather_ref(c1, vbase + (size_t)(field - SES3D_FIELD_VX) * G, tmp, h->st);
+    if (e != cudaSuccess) return done(cuda_fail(h, e, "gather"));
+    e = cudaMemcpyAsync(hout, tmp, N * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e != cudaSuccess) return done(cuda_fail(h, e, "copy"));
+  } else if (state_field_index(field) >= 0) {
+    float *d = sbase + (size_t)state_field_index(field) * N;
+    cudaError_t e;
+    if (hout) {
+      e = launch_transpose(d, tmp, h->geo.E, NPE, h->st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(hout, tmp, N * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    } else {
+      e = cudaMemcpyAsync(tmp, hin, N * sizeof(float), cudaMemcpyHostToDevice, h->st);
+      if (e == cudaSuccess) e = launch_transpose(tmp, d, NPE, h->geo.E, h->st);
+    }
+    if (e != cudaSuccess) return done(cuda_fail(h, e, "field transfer"));
+  } else if (field >= SES3D_FIELD_MXX && field <= SES3D_FIELD_MYZ) {
+    const int cc = field - SES3D_FIELD_MXX;
+    std::vector<float> buf((size_t)N), inter;
+    if (hout) {
+      for (int m = 0; m < 3; ++m) {
+        cudaError_t e = launch_transpose(sbase + (size_t)(F_M + 3 * cc + m) * N, tmp, h->geo.E, NPE, h->st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(buf.data(), tmp, N * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+        if (e != cudaSuccess) return done(cuda_fail(h, e, "memory variable transfer"));
+        for (long long q = 0; q < N; ++q) hout[m + 3 * q] = buf[q];
+      }
+    } else {
+      for (int m = 0; m < 3; ++m) {
+        for (long long q = 0; q < N; ++q) buf[q] = hin[m + 3 * q];
+        cudaError_t e = cudaMemcpyAsync(tmp, buf.data(), N * sizeof(float), cudaMemcpyHostToDevice, h->st);
+        if (e == cudaSuccess) e = launch_transpose(tmp, sbase + (size_t)(F_M + 3 * cc + m) * N, NPE, h->geo.E, h->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+        if (e != cudaSuccess) return done(cuda_fail(h, e, "memory variable transfer"));
+      }
+    }
+  } else {
+    out_rc = fail(h, SES3D_E_CONFIG, "unknown field");
+  }
+  cudaError_t e = cudaStreamSynchronize(h->st);
+  if (e != cudaSuccess) return done(cuda_fail(h, e, "field sync"));
+  destroy_graph(h);
+  return done(out_rc);
+}
+
+int ses3d_gpu_get_field(ses3d_gpu *h, int event, int field, float *out) {
+  if (!out) return fail(h, SES3D_E_CONFIG, "null output");
+  return field_io(h, event, field, out, nullptr);
+}
+
+int ses3d_gpu_set_field(ses3d_gpu *h, int event, int field, const float *in) {
+  if (!in) return fail(h, SES3D_E_CONFIG, "null input");
+  return field_io(h, event, field, nullptr, in);
+}
+
+int ses3d_gpu_get_kernel(ses3d_gpu *h, int event, int which, double *out) {
+  int rc = check_event(h, event);
+  if (rc) return rc;
+  if (which < 0 || which >= SES3D_KERNEL_COUNT || !out) return fail(h, SES3D_E_CONFIG, "bad kernel id");
+  if (!h->d_grad) return fail(h, SES3D_E_STATE, "kernels exist only in adjoint runs (adjoint_flag = 2)");
+  const long long N = h->geo.N;
+  static const int slot[] = {0, 1, 2, 3, 4, 5, 6, 7};
+  double *tmp = nullptr;
+  CK(h, dalloc(&tmp, (size_t)N));
+  cudaError_t e = launch_transpose_d(h->d_grad + ((size_t)event * NGRAD + slot[which]) * N, tmp, h->geo.E, NPE, h->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, tmp, N * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  dfree(tmp);
+  if (e != cudaSuccess) return cuda_fail(h, e, "get_kernel");
+  return SES3D_OK;
+}
+
+int ses3d_gpu_record_count(const ses3d_gpu *h, int event) {
+  if (!h || event < 0 || event >= h->cfg.n_events) return SES3D_E_CONFIG;
+  return (int)h->records.size();
+}
+
+int ses3d_gpu_get_record(ses3d_gpu *h, int event, int record, float *out) {
+  int rc = check_event(h, event);
+  if (rc) return rc;
+  if (record < 0 || record >= (int)h->records.size() || !out) return fail(h, SES3D_E_CONFIG, "bad record index");
+  const long long N = h->geo.N;
+  float *tmp = nullptr;
+  CK(h, dalloc(&tmp, (size_t)N));
+  cudaError_t e = cudaSuccess;
+  for (int f = 0; f < NREC && e == cudaSuccess; ++f) {
+    e = launch_transpose(h->records[record] + ((size_t)event * NREC + f) * N, tmp, h->geo.E, NPE, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out + (size_t)f * N, tmp, N * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  }
+  dfree(tmp);
+  if (e != cudaSuccess) return cuda_fail(h, e, "get_record");
+  return SES3D_OK;
+}
+
+int ses3d_gpu_put_record(ses3d_gpu *h, int event, int record, const float *in) {
+  int rc = check_event(h, event);
+  if (rc) return rc;
+  if (record < 0 || record > (int)h->records.size() || !in) return fail(h, SES3D_E_CONFIG, "bad record index");
+  const long long N = h->geo.N;
+  if (record == (int)h->records.size()) {
+    float *r = nullptr;
+    CK(h, dalloc(&r, (size_t)h->cfg.n_events * NREC * N));
+    CK(h, cudaMemset(r, 0, (size_t)h->cfg.n_events * NREC * N * sizeof(float)));
+    h->records.push_back(r);
+    h->record_cursor = (int)h->records.size();
+  }
+  float *tmp = nullptr;
+  CK(h, dalloc(&tmp, (size_t)N));
+  cudaError_t e = cudaSuccess;
+  for (int f = 0; f < NREC && e == cudaSuccess; ++f) {
+    e = cudaMemcpyAsync(tmp, in + (size_t)f * N, N * sizeof(float), cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = launch_transpose(tmp, h->records[record] + ((size_t)event * NREC + f) * N, NPE, h->geo.E, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  }
+  dfree(tmp);
+  if (e != cudaSuccess) return cuda_fail(h, e, "put_record");
+  return SES3D_OK;
+}
+
+int ses3d_gpu_get_saving_vector(const ses3d_gpu *h, int *out) {
+  if (!h || !out) return SES3D_E_CONFIG;
+  for (int k = 1; k <= h->cfg.nt; ++k) out[k - 1] = h->saving_vector[k];
+  return SES3D_OK;
+}
+
+int ses3d_gpu_set_saving_vector(ses3d_gpu *h, const int *in) {
+  if (!h || !in) return SES3D_E_CONFIG;
+  for (int k = 1; k <= h->cfg.nt; ++k) h->saving_vector[k] = in[k - 1];
+  return SES3D_OK;
+}
+
+int ses3d_gpu_begin_adjoint(ses3d_gpu *h) {
+  if (!h) return SES3D_E_CONFIG;
+  h->mode_flag = 2;
+  h->cfg.adjoint_flag = 2;
+  if (!h->d_grad) {
+    CK(h, dalloc(&h->d_grad, (size_t)h->cfg.n_events * NGRAD * h->geo.N));
+  }
+  CK(h, cudaMemsetAsync(h->d_grad, 0, (size_t)h->cfg.n_events * NGRAD * h->geo.N * sizeof(double), h->st));
+  h->record_cursor = (int)h->records.size();
+  int rc = zero_wavefield(h);
+  if (rc) return rc;
+  rc = upload_moment_sources(h);
+  if (rc) return rc;
+  rc = rebuild_forces(h);
+  if (rc) return rc;
+  CK(h, cudaStreamSynchronize(h->st));
+  return SES3D_OK;
+}
+
+long ses3d_gpu_get_setup_int(ses3d_gpu *h, int event, const char *name, int *out) {
+  int rc = check_event(h, event);
+  if (rc) return rc;
+  const std::string nm = name ? name : "";
+  const EventHost &E = h->ev[event];
+  auto one = [&](int v) -> long { if (out) out[0] = v; return 1; };
+  auto vec = [&](const std::vector<int> &v) -> long { if (out) std::copy(v.begin(), v.end(), out); return (long)v.size(); };
+  if (nm == "nr") return one((int)E.recs.size());
+  if (nm == "rx" || nm == "ry" || nm == "rz") {
+    std::vector<int> v;
+    for (const Receiver &r : E.recs) v.push_back(nm == "rx" ? r.rx : nm == "ry" ? r.ry : r.rz);
+    return vec(v);
+  }
+  if (nm == "kept") { std::vector<int> v; for (const Receiver &r : E.recs) v.push_back(r.global_index); return vec(v); }
+  if (nm == "isx") return one(E.src.isx);
+  if (nm == "isy") return one(E.src.isy);
+  if (nm == "isz") return one(E.src.isz);
+  if (nm == "isx_n") return one(E.src.isx_n);
+  if (nm == "isy_n") return one(E.src.isy_n);
+  if (nm == "isz_n") return one(E.src.isz_n);
+  if (nm == "is_source") return one(E.src.is_source);
+  if (nm == "nr_adsrc") return one((int)E.adj.size());
+  if (nm == "is" || nm == "isn") {
+    std::vector<int> v;
+    for (const AdjointSource &a : E.adj)
+      for (int c = 0; c < 3; ++c) v.push_back(nm == "is" ? a.is[c] : a.isn[c]);
+    return vec(v);
+  }
+  return fail(h, SES3D_E_CONFIG, "unknown setup integer " + nm);
+}
+
+long ses3d_gpu_get_setup_real(ses3d_gpu *h, int event, const char *name, float *out) {
+  int rc = check_event(h, event);
+  if (rc) return rc;
+  const std::string nm = name ? name : "";
+  const EventHost &E = h->ev[event];
+  const Geometry &g = h->geo;
+  auto one = [&](float v) -> long { if (out) out[0] = v; return 1; };
+  auto vec = [&](const std::vector<float> &v) -> long { if (out) std::copy(v.begin(), v.end(), out); return (long)v.size(); };
+  if (nm == "xxs_loc") return one(E.src.xxs_loc);
+  if (nm == "yys_loc") return one(E.src.yys_loc);
+  if (nm == "zzs_loc") return one(E.src.zzs_loc);
+  if (nm == "dx") return one(g.dx);
+  if (nm == "dy") return one(g.dy);
+  if (nm == "dz") return one(g.dz);
+  if (nm == "Jac") return one(g.Jac);
+  if (nm == "knots") return vec(std::vector<float>(g.knots, g.knots + NP));
+  if (nm == "w") return vec(std::vector<float>(g.w, g.w + NP));
+  if (nm == "dl") {  // F-order (i,j): dl(i,j) at i + 5 j
+    std::vector<float> v(NP * NP);
+    for (int i = 0; i < NP; ++i) for (int j = 0; j < NP; ++j) v[i + NP * j] = g.dl[i][j];
+    return vec(v);
+  }
+  auto axis = [&](const std::vector<float> &t, int ne) {  // (0:ne-1, 0:lpd) F-order
+    std::vector<float> v((size_t)ne * NP);
+    for (int i = 0; i < ne; ++i) for (int n = 0; n < NP; ++n) v[i + (size_t)ne * n] = t[(size_t)i * NP + n];
+    return v;
+  };
+  if (nm == "x") return vec(axis(g.x, g.ex));
+  if (nm == "y") return vec(axis(g.y, g.ey));
+  if (nm == "z") return vec(axis(g.z, g.ez));
+  if (nm == "recloc_std") {
+    std::vector<float> v;
+    for (const Receiver &r : E.recs) v.insert(v.end(), r.std, r.std + 3);
+    return vec(v);
+  }
+  if (nm == "ad_loc_std") {
+    std::vector<float> v;
+    for (const AdjointSource &a : E.adj) v.insert(v.end(), a.loc_std, a.loc_std + 3);
+    return vec(v);
+  }
+  if (nm == "prof_x" || nm == "prof_y" || nm == "prof_z" || nm == "prof" || nm == "taper") {
+    if (!out) return (long)g.N;
+    for (int kn = 0; kn < NP; ++kn)
+      for (int jn = 0; jn < NP; ++jn)
+        for (int in = 0; in < NP; ++in)
+          for (int k = 0; k < g.ez; ++k)
+            for (int j = 0; j < g.ey; ++j)
+              for (int i = 0; i < g.ex; ++i) {
+                float px, py, pz, prof, taper;
+                pml_normalise(g.pxr[(size_t)i * NP + in], g.pyr[(size_t)j * NP + jn], g.pzr[(size_t)k * NP + kn],
+                              px, py, pz, prof, taper);
+                long long e = i + (long long)g.ex * (j + (long long)g.ey * k);
+                long long q = e + g.E * (in + NP * (jn + NP * kn));
+                out[q] = nm == "prof_x" ? px : nm == "prof_y" ? py : nm == "prof_z" ? pz : nm == "prof" ? prof : taper;
+              }
+    return (long)g.N;
+  }
+  return fail(h, SES3D_E_CONFIG, "unknown setup real " + nm);
+}
+
+int ses3d_gpu_vmax(ses3d_gpu *h, float *out) {
+  if (!h || !out) return SES3D_E_CONFIG;
+  const int nev = h->cfg.n_events;
+  CK(h, cudaMemsetAsync(h->d_scratch_u, 0, nev * sizeof(unsigned int), h->st));
+  CK(h, launch_vmax(h->d_v, 3 * h->geo.G, nev, h->d_scratch_u, h->st));
+  ++h->launches;
+  std::vector<unsigned int> u(nev);
+  CK(h, cudaMemcpyAsync(u.data(), h->d_scratch_u, nev * sizeof(unsigned int), cudaMemcpyDeviceToHost, h->st));
+  CK(h, cudaStreamSynchronize(h->st));
+  bool bad = false;
+  for (int e = 0; e < nev; ++e) {
+    std::memcpy(&out[e], &u[e], sizeof(float));
+    if (!(out[e] < 3.0e38f)) bad = true;
+  }
+  if (bad) return fail(h, SES3D_E_NAN, "non-finite velocity field");
+  return SES3D_OK;
+}
+
+void *ses3d_gpu_stream(ses3d_gpu *h) { return h ? (void *)h->st : nullptr; }
+
+int64_t ses3d_gpu_launch_count(const ses3d_gpu *h) { return h ? h->launches : 0; }
+
+int ses3d_gpu_use_graph(ses3d_gpu *h, int enable, int n_per_graph) {
+  if (!h) return SES3D_E_CONFIG;
+  if (enable && n_per_graph < 1) return fail(h, SES3D_E_CONFIG, "n_per_graph must be >= 1");
+  destroy_graph(h);
+  h->graph_on = enable != 0;
+  h->graph_n = enable ? n_per_graph : 0;
+  return SES3D_OK;
+}
+
+int ses3d_gpu_profile(ses3d_gpu *h, int enable) {
+  if (!h) return SES3D_E_CONFIG;
+  h->prof_on = enable != 0;
+  if (enable)
+    for (int k = 0; k < 4; ++k) { h->prof_ms[k] = 0; h->prof_n[k] = 0; }
+  return SES3D_OK;
+}
+
+int ses3d_gpu_kernel_time(const ses3d_gpu *h, int which, double *total_ms, int64_t *launches) {
+  if (!h || which < 0 || which > 3) return SES3D_E_CONFIG;
+  if (total_ms) *total_ms = h->prof_ms[which];
+  if (launches) *launches = h->prof_n[which];
+  return SES3D_OK;
+}
+
+int ses3d_gpu_set_block_elements(ses3d_gpu *h, int elements_per_cta) {
+  if (!h) return SES3D_E_CONFIG;
+  if (elements_per_cta == 0) elements_per_cta = 1;
+  if (elements_per_cta != 1 && elements_per_cta != 2 && elements_per_cta != 4)
+    return fail(h, SES3D_E_CONFIG, "elements_per_cta must be 1, 2 or 4");
+  h->epb = elements_per_cta;
+  destroy_graph(h);
+  return SES3D_OK;
+}
+
+}  // extern "C"

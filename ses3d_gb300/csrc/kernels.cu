@@ -1,0 +1,621 @@
+// kernels.cu -- sm_103a kernels of the SES3D time step.
+//
+// One iteration of SOURCE/ses3d_evolution.f90 is three launches:
+//   k_receivers  record_seismograms on the pre-update velocity (ses3d_output.f90:456-497)
+//   k_element    everything element-local: gather, strain rates, spherical terms,
+//                displacement gradients, PML strain, stress rates, memory variables,
+//                PML stress march, moment source, weak divergence, taper
+//                (ses3d_evolution.f90:27-271,334-360,368-371; ses3d_miscellaneous.f90:97-150)
+//   k_inject     single-force / adjoint forces into the element forces (ses3d_miscellaneous.f90:11-94)
+//   k_node       deterministic assembly, mass matrix, leapfrog, taper (ses3d_evolution.f90:282-328,366)
+// The MPI face exchange of the reference (ses3d_miscellaneous.f90:257-368) becomes the
+// node-centric gather of k_node: each global node sums its (up to 8) element
+// contributions in the reference loop order, without atomics, so runs are bit-reproducible.
+#include "kernels.cuh"
+
+namespace ses3d {
+
+// ---------------------------------------------------------------------------------------
+// k_element: one element per 128 threads (thread = GLL node), EPB elements per CTA.
+// MODE 0 plain, 1 store forward record, 2 adjoint with kernel correlation.
+// ---------------------------------------------------------------------------------------
+template <bool DISS, int MODE, int EPB>
+__global__ void __launch_bounds__(TPE * EPB) k_element(const Consts c, const Ptrs p) {
+  __shared__ KTab tab;
+  __shared__ float s_v[EPB][3][TPE];
+  __shared__ float s_p[EPB][9][TPE];
+
+  for (int t = threadIdx.x; t < KTAB_FLOATS; t += blockDim.x)
+    reinterpret_cast<float *>(&tab)[t] = reinterpret_cast<const float *>(p.ktab)[t];
+
+  const int sub = threadIdx.x / TPE;
+  const int n = threadIdx.x % TPE;
+  const long long blk = (long long)blockIdx.x * EPB + sub;
+  const bool blk_ok = blk < c.E * c.nev;
+  const int ev = blk_ok ? (int)(blk % c.nev) : 0;
+  const long long e = blk_ok ? blk / c.nev : 0;
+  const bool act = blk_ok && n < 125;
+  const int nn = act ? n : 0;
+  const int in = nn % 5, jn = (nn / 5) % 5, kn = nn / 25;
+  const int i = (int)(e % c.ex);
+  const int j = (int)((e / c.ex) % c.ey);
+  const int k = (int)(e / ((long long)c.ex * c.ey));
+  const long long N = c.N;
+
+  // gather v_global -> element-local v (ses3d_evolution.f90:27-51)
+  float vx = 0.f, vy = 0.f, vz = 0.f;
+  if (act) {
+    const long long g = (long long)(i * 4 + in) + (long long)c.GX * ((j * 4 + jn) + (long long)c.GY * (k * 4 + kn));
+    const float *v = p.v + (long long)ev * 3 * c.G;
+    vx = v[g]; vy = v[c.G + g]; vz = v[2 * c.G + g];
+  }
+  s_v[sub][0][n] = vx; s_v[sub][1][n] = vy; s_v[sub][2][n] = vz;
+  __syncthreads();
+
+  const long long q0 = (long long)ev * NSTATE * N + e * 125 + nn;  // state field 0 of this node
+  float *S = p.state + q0;
+  const long long m0 = e * 125 + nn;  // material / element-local index
+
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  float r = 1.f, st = 1.f;
+  if (act) {
+    // strain-rate proxies (ses3d_evolution.f90:57-87)
+    float exx = 0.f, exy = 0.f, exz = 0.f, eyx = 0.f, eyy = 0.f, eyz = 0.f, ezx = 0.f, ezy = 0.f, ezz = 0.f;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      const int ix = q + 5 * jn + 25 * kn, iy = in + 5 * q + 25 * kn, iz = in + 5 * jn + 25 * q;
+      const float dxq = tab.Dx[in][q], dyq = tab.Dy[jn][q], dzq = tab.Dz[kn][q];
+      exx = fmaf(s_v[sub][0][ix], dxq, exx);
+      exy = fmaf(s_v[sub][1][ix], dxq, exy);
+      exz = fmaf(s_v[sub][2][ix], dxq, exz);
+      eyx = fmaf(s_v[sub][0][iy], dyq, eyx);
+      eyy = fmaf(s_v[sub][1][iy], dyq, eyy);
+      eyz = fmaf(s_v[sub][2][iy], dyq, eyz);
+      ezx = fmaf(s_v[sub][0][iz], dzq, ezx);
+      ezy = fmaf(s_v[sub][1][iz], dzq, ezy);
+      ezz = fmaf(s_v[sub][2][iz], dzq, ezz);
+    }
+    // spherical completion (ses3d_evolution.f90:93-103)
+    r = __ldg(p.r_z + k * 5 + kn);
+    st = __ldg(p.sin_x + i * 5 + in);
+    const float ct = __ldg(p.cot_x + i * 5 + in);
+    const float rs = r * st;
+    ezz = -ezz;
+    eyy = eyy / rs + (vz + vx * ct) / r;
+    exx = (vz + exx) / r;
+    ezx = -ezx;
+    exz = (exz - vx) / r;
+    ezy = -ezy;
+    eyz = -vy / r + eyz / rs;
+    exy = exy / r;
+    eyx = -vy * ct / r + eyx / rs;
+    // displacement gradients (ses3d_evolution.f90:109-117)
+    const float dt = c.dt;
+    const float dxux = S[F_DXUX * N] + dt * exx, dyuy = S[F_DYUY * N] + dt * eyy, dzuz = S[F_DZUZ * N] + dt * ezz;
+    const float dxuy = S[F_DXUY * N] + dt * exy, dyux = S[F_DYUX * N] + dt * eyx;
+    const float dxuz = S[F_DXUZ * N] + dt * exz, dzux = S[F_DZUX * N] + dt * ezx;
+    const float dyuz = S[F_DYUZ * N] + dt * eyz, dzuy = S[F_DZUY * N] + dt * ezy;
+    S[F_DXUX * N] = dxux; S[F_DYUY * N] = dyuy; S[F_DZUZ * N] = dzuz;
+    S[F_DXUY * N] = dxuy; S[F_DYUX * N] = dyux; S[F_DXUZ * N] = dxuz;
+    S[F_DZUX * N] = dzux; S[F_DYUZ * N] = dyuz; S[F_DZUY * N] = dzuy;
+    // PML profiles of this node (ses3d_init.f90:678-686), corners normalised
+    const float pxr = __ldg(p.pxr + i * 5 + in), pyr = __ldg(p.pyr + j * 5 + jn), pzr = __ldg(p.pzr + k * 5 + kn);
+    float px = 0.f, py = 0.f, pz = 0.f, taper = 1.f;
+    const float praw = __fadd_rn(__fadd_rn(pxr, pyr), pzr);
+    if (praw != 0.f) {
+      const float den = __fadd_rn(1.f, __fdiv_rn(praw, 1.2f));
+      pz = __fdiv_rn(__fmul_rn(2.f, pzr), den);
+      py = __fdiv_rn(__fmul_rn(2.f, pyr), den);
+      px = __fdiv_rn(__fmul_rn(2.f, pxr), den);
+      const float prof = __fadd_rn(__fadd_rn(px, py), pz);
+      taper = expf(-__fmul_rn(__fmul_rn(0.1f, prof), prof));
+    }
+    // PML strain rates and symmetrisation (ses3d_evolution.f90:123-138)
+    exx = exx + (pz + py) * dxux;
+    eyy = eyy + (px + pz) * dyuy;
+    ezz = ezz + (px + py) * dzuz;
+    exy = exy + (py + pz) * dxuy;
+    eyx = eyx + (px + pz) * dyux;
+    exz = exz + (py + pz) * dxuz;
+    ezx = ezx + (px + py) * dzux;
+    eyz = eyz + (px + pz) * dyuz;
+    ezy = ezy + (px + py) * dzuy;
+    exy = (exy + eyx) * 0.5f;
+    exz = (exz + ezx) * 0.5f;
+    eyz = (eyz + ezy) * 0.5f;
+    // stress rates (ses3d_evolution.f90:146-202)
+    const float *MT = p.mat + m0;
+    const float clam = __ldg(MT + M_CLAM * N), c2mut = __ldg(MT + M_C2MUT * N);
+    const float cA = __ldg(MT + M_A * N), cB2 = __ldg(MT + M_B2 * N), cC = __ldg(MT + M_C * N);
+    const float tr = exx + eyy + ezz;
+    float sxx, syy, szz, sxy, sxz, syz;
+    float Mv[18];
+    if (DISS) {
+      const float c2mt = __ldg(MT + M_C2MT * N);
+#pragma unroll
+      for (int t = 0; t < 18; ++t) Mv[t] = S[(F_M + t) * N];
+      const float Mdx = Mv[0] + Mv[1] + Mv[2], Mdy = Mv[3] + Mv[4] + Mv[5], Mdz = Mv[6] + Mv[7] + Mv[8];
+      const float Mxy = Mv[9] + Mv[10] + Mv[11], Mxz = Mv[12] + Mv[13] + Mv[14], Myz = Mv[15] + Mv[16] + Mv[17];
+      const float Lw = clam * tr - c2mt * (Mdx + Mdy + Mdz) * (1.f / 3.f);
+      sxx = Lw + c2mut * exx + c2mt * Mdx + cC * ezz + cA * (eyy + exx);
+      syy = Lw + c2mut * eyy + c2mt * Mdy + cC * ezz + cA * (eyy + exx);
+      szz = Lw + c2mut * ezz + c2mt * Mdz + cC * (eyy + exx);
+      sxy = c2mut * exy + c2mt * Mxy;
+      sxz = c2mut * exz + c2mt * Mxz + cB2 * exz;
+      syz = c2mut * eyz + c2mt * Myz + cB2 * eyz;
+      // memory variables with the PML-modified, symmetrised strain rates (ses3d_evolution.f90:334-360)
+      const float ecomp[6] = {exx, eyy, ezz, exy, exz, eyz};
+#pragma unroll
+      for (int cc = 0; cc < 6; ++cc)
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          float M = Mv[3 * cc + m];
+          M = M - M * c.a_k[m] - c.L_k[m] * ecomp[cc];
+          Mv[3 * cc + m] = M;
+          S[(F_M + 3 * cc + m) * N] = M;
+        }
+    } else {
+      const float Lw = clam * tr;
+      sxx = Lw + c2mut * exx + cC * ezz + cA * (eyy + exx);
+      syy = Lw + c2mut * eyy + cC * ezz + cA * (eyy + exx);
+      szz = Lw + c2mut * ezz + cC * (eyy + exx);
+      sxy = c2mut * exy;
+      sxz = c2mut * exz + cB2 * exz;
+      syz = c2mut * eyz + cB2 * eyz;
+    }
+    // march PML stresses (ses3d_evolution.f90:208-219)
+    float s_xx = S[F_SXX * N], s_yy = S[F_SYY * N], s_zz = S[F_SZZ * N];
+    float s_xy = S[F_SXY * N], s_yx = S[F_SYX * N], s_xz = S[F_SXZ * N];
+    float s_zx = S[F_SZX * N], s_yz = S[F_SYZ * N], s_zy = S[F_SZY * N];
+    s_xx = s_xx + dt * (sxx - px * s_xx);
+    s_yy = s_yy + dt * (syy - py * s_yy);
+    s_zz = s_zz + dt * (szz - pz * s_zz);
+    s_xy = s_xy + dt * (sxy - px * s_xy);
+    s_yx = s_yx + dt * (sxy - py * s_yx);
+    s_xz = s_xz + dt * (sxz - px * s_xz);
+    s_zx = s_zx + dt * (sxz - pz * s_zx);
+    s_yz = s_yz + dt * (syz - py * s_yz);
+    s_zy = s_zy + dt * (syz - pz * s_zy);
+    // taper (ses3d_evolution.f90:368-371); the divergence below uses the untapered values
+    S[F_SXX * N] = s_xx * taper; S[F_SYY * N] = s_yy * taper; S[F_SZZ * N] = s_zz * taper;
+    S[F_SXY * N] = s_xy * taper; S[F_SYX * N] = s_yx * taper; S[F_SXZ * N] = s_xz * taper;
+    S[F_SZX * N] = s_zx * taper; S[F_SYZ * N] = s_yz * taper; S[F_SZY * N] = s_zy * taper;
+    // moment-tensor source field (ses3d_miscellaneous.f90:115-147)
+    if (MODE != 2 && e == (long long)__ldg(p.src_elem + ev)) {
+      const int it = *p.d_it + 1;
+      const float d = p.src_delta[ev * 125 + nn];
+      const float so = p.stf[(long long)ev * c.nt + (it - 1)];
+      const float *mom = p.src_mom + ev * 6;
+      const float sxxs = -(__fmul_rn(__fmul_rn(mom[0], d), so)), syys = -(__fmul_rn(__fmul_rn(mom[1], d), so));
+      const float szzs = -(__fmul_rn(__fmul_rn(mom[2], d), so)), sxys = -(__fmul_rn(__fmul_rn(mom[3], d), so));
+      const float sxzs = -(__fmul_rn(__fmul_rn(mom[4], d), so)), syzs = -(__fmul_rn(__fmul_rn(mom[5], d), so));
+      s_xx += sxxs; s_yy += syys; s_zz += szzs;
+      s_xy += sxys; s_yx += sxys; s_xz += sxzs; s_zx += sxzs; s_yz += syzs; s_zy += syzs;
+    }
+    // node-local weights of the weak divergence (ses3d_evolution.f90:247-249)
+    const float wx = tab.w[in] * st, wy = tab.w[jn], wz = tab.w[kn] * r * r;
+    s_p[sub][0][n] = wx * s_xx; s_p[sub][1][n] = wx * s_xy; s_p[sub][2][n] = wx * s_xz;
+    s_p[sub][3][n] = wy * s_yx; s_p[sub][4][n] = wy * s_yy; s_p[sub][5][n] = wy * s_yz;
+    s_p[sub][6][n] = wz * s_zx; s_p[sub][7][n] = wz * s_zy; s_p[sub][8][n] = wz * s_zz;
+
+    if (MODE == 1) {  // forward record (ses3d_main.f90:148-158)
+      float *R = p.rec + (long long)ev * NREC * N + m0;
+      R[R_VX * N] = vx; R[R_VY * N] = vy; R[R_VZ * N] = vz;
+      R[R_EXX * N] = dxux; R[R_EYY * N] = dyuy; R[R_EZZ * N] = dzuz;
+      R[R_EXY * N] = (dxuy + dyux) / 2.f; R[R_EXZ * N] = (dxuz + dzux) / 2.f; R[R_EYZ * N] = (dyuz + dzuy) / 2.f;
+    }
+    if (MODE == 2 && p.rec) {  // kernel correlation (ses3d_grad.f90:53-83, ses3d_grad_Q.f90:111-143)
+      const float *R = p.rec + (long long)ev * NREC * N + m0;
+      const float vxf = R[R_VX * N], vyf = R[R_VY * N], vzf = R[R_VZ * N];
+      const float exxf = R[R_EXX * N], eyyf = R[R_EYY * N], ezzf = R[R_EZZ * N];
+      const float exyf = R[R_EXY * N], exzf = R[R_EXZ * N], eyzf = R[R_EYZ * N];
+      const float exx_ad = dxux, eyy_ad = dyuy, ezz_ad = dzuz;
+      const float exy_ad = 0.5f * (dxuy + dyux), exz_ad = 0.5f * (dxuz + dzux), eyz_ad = 0.5f * (dyuz + dzuy);
+      const float tr_ad = exx_ad + eyy_ad + ezz_ad, tr_fw = exxf + eyyf + ezzf;
+      const float edde = exx_ad * exxf + eyy_ad * eyyf + ezz_ad * ezzf + 2.f * exy_ad * exyf +
+                         2.f * exz_ad * exzf + 2.f * eyz_ad * eyzf;
+      const float *GM = p.gmat + m0;
+      const float rho = GM[G_RHO * N], cp = GM[G_CP * N], cs = GM[G_CS * N];
+      const double sj = (double)c.s_grad / (double)c.Jac;
+      double *GR = p.grad + (long long)ev * NGRAD * N + m0;
+      GR[0 * N] += sj * (double)((vxf * vx + vyf * vy + vzf * vz) +
+                                 ((cp * cp - 2.f * cs * cs) * tr_fw * tr_ad + 2.f * cs * cs * edde));
+      GR[1 * N] += sj * (double)(2.f * rho * cp * tr_fw * tr_ad);
+      GR[2 * N] += sj * (double)(4.f * rho * cs * (edde - tr_ad * tr_fw - 2.f * exzf * exz_ad - 2.f * eyzf * eyz_ad));
+      GR[3 * N] += sj * (double)(8.f * rho * cs * (exzf * exz_ad + eyzf * eyz_ad));
+      if (DISS && p.grad_q) {
+        const float dPdalpha[3] = {-3.06f, -1.54f, 2.56f};
+        const float ef[6] = {exxf, eyyf, ezzf, exyf, exzf, eyzf};
+        double gq = 0.0, ga = 0.0, gk = 0.0, gak = 0.0;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          const float tsum = Mv[m] + Mv[3 + m] + Mv[6 + m];
+          float Md = 0.f;
+#pragma unroll
+          for (int cc = 0; cc < 6; ++cc) Md += Mv[3 * cc + m] * ef[cc];
+          Md = Md - tr_fw * tsum / 3.f;
+          gq += (double)(Md * c.tau_p[m]);
+          ga += (double)(Md * dPdalpha[m] * c.tau_p[m] / c.D_p[m]);
+          const float Mk = tsum * tr_fw;
+          gk += (double)(Mk * c.tau_p[m]);
+          gak += (double)(Mk * dPdalpha[m] * c.tau_p[m] / c.D_p[m]);
+        }
+        GR[4 * N] += sj * gq;
+        GR[5 * N] += sj * ga;
+        GR[6 * N] += sj * gk;
+        GR[7 * N] += sj * gak;
+      }
+    }
+  }
+  __syncthreads();
+
+  if (act) {
+    // weak-form divergence (ses3d_evolution.f90:235-270)
+    float ax0 = 0.f, ax1 = 0.f, ax2 = 0.f, ay0 = 0.f, ay1 = 0.f, ay2 = 0.f, az0 = 0.f, az1 = 0.f, az2 = 0.f;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      const int ix = q + 5 * jn + 25 * kn, iy = in + 5 * q + 25 * kn, iz = in + 5 * jn + 25 * q;
+      const float dxq = tab.dlT[in][q], dyq = tab.dlT[jn][q], dzq = tab.dlT[kn][q];
+      ax0 = fmaf(s_p[sub][0][ix], dxq, ax0);
+      ax1 = fmaf(s_p[sub][1][ix], dxq, ax1);
+      ax2 = fmaf(s_p[sub][2][ix], dxq, ax2);
+      ay0 = fmaf(s_p[sub][3][iy], dyq, ay0);
+      ay1 = fmaf(s_p[sub][4][iy], dyq, ay1);
+      ay2 = fmaf(s_p[sub][5][iy], dyq, ay2);
+      az0 = fmaf(s_p[sub][6][iz], dzq, az0);
+      az1 = fmaf(s_p[sub][7][iz], dzq, az1);
+      az2 = fmaf(s_p[sub][8][iz], dzq, az2);
+    }
+    const float cx = tab.CX[jn][kn] * r, cy = tab.CY[in][kn] * r, cz = tab.CZ[in][jn] * st;
+    fx = cx * ax0 + cy * ay0 + cz * az0;
+    fy = cx * ax1 + cy * ay1 + cz * az1;
+    fz = cx * ax2 + cy * ay2 + cz * az2;
+    float *F = p.f + (long long)ev * 3 * N + m0;
+    F[0] = fx; F[N] = fy; F[2 * N] = fz;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// k_node: one thread per (global node, event). Deterministic assembly in the reference
+// order (element i, then j, then k ascending; ses3d_evolution.f90:286-310), then
+// a = s / MM, v += dt (a - prof v), v *= taper (ses3d_evolution.f90:318-328,366).
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_node(const Consts c, const Ptrs p) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int ev = blockIdx.y;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *p.d_it += 1;  // all readers finished earlier in stream order
+  if (g >= c.G) return;
+  const int gx = (int)(g % c.GX);
+  const int gy = (int)((g / c.GX) % c.GY);
+  const int gz = (int)(g / ((long long)c.GX * c.GY));
+  const int i0 = gx == 0 ? 0 : (gx - 1) >> 2, i1 = min(gx >> 2, c.ex - 1);
+  const int j0 = gy == 0 ? 0 : (gy - 1) >> 2, j1 = min(gy >> 2, c.ey - 1);
+  const int k0 = gz == 0 ? 0 : (gz - 1) >> 2, k1 = min(gz >> 2, c.ez - 1);
+  const long long N = c.N;
+  const float *F = p.f + (long long)ev * 3 * N;
+  float sx = 0.f, sy = 0.f, sz = 0.f;
+  for (int i = i0; i <= i1; ++i)
+    for (int j = j0; j <= j1; ++j)
+      for (int k = k0; k <= k1; ++k) {
+        const long long q = ((long long)i + (long long)c.ex * (j + (long long)c.ey * k)) * 125 +
+                            (gx - 4 * i) + 5 * (gy - 4 * j) + 25 * (gz - 4 * k);
+        sx += F[q]; sy += F[N + q]; sz += F[2 * N + q];
+      }
+  const float mm = p.MM[g];
+  const float ax = sx / mm, ay = sy / mm, az = sz / mm;
+  const float pxr = __ldg(p.pxg + gx), pyr = __ldg(p.pyg + gy), pzr = __ldg(p.pzg + gz);
+  float prof = 0.f, taper = 1.f;
+  const float praw = __fadd_rn(__fadd_rn(pxr, pyr), pzr);
+  if (praw != 0.f) {
+    const float den = __fadd_rn(1.f, __fdiv_rn(praw, 1.2f));
+    const float pz = __fdiv_rn(__fmul_rn(2.f, pzr), den);
+    const float py = __fdiv_rn(__fmul_rn(2.f, pyr), den);
+    const float px = __fdiv_rn(__fmul_rn(2.f, pxr), den);
+    prof = __fadd_rn(__fadd_rn(px, py), pz);
+    taper = expf(-__fmul_rn(__fmul_rn(0.1f, prof), prof));
+  }
+  float *V = p.v + (long long)ev * 3 * c.G + g;
+  const float dt = c.dt;
+  float vx = V[0], vy = V[c.G], vz = V[2 * c.G];
+  vx = vx + dt * (ax - prof * vx);
+  vy = vy + dt * (ay - prof * vy);
+  vz = vz + dt * (az - prof * vz);
+  V[0] = taper * vx; V[c.G] = taper * vy; V[2 * c.G] = taper * vz;
+}
+
+// ---------------------------------------------------------------------------------------
+// k_receivers: one warp per receiver; Lagrange interpolation of the pre-update local
+// velocity (ses3d_output.f90:475-493). Fixed lane order + xor tree: deterministic.
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_receivers(const Consts c, const float *__restrict__ v,
+                                                   const int *__restrict__ rec_elem, const int *__restrict__ rec_ev,
+                                                   const float *__restrict__ rec_w, float *__restrict__ seis, int R,
+                                                   const int *__restrict__ d_it) {
+  const int r = blockIdx.x * 4 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= R) return;
+  const int it = *d_it + 1;
+  const long long e = rec_elem[r];
+  const int ev = rec_ev[r];
+  const int i = (int)(e % c.ex), j = (int)((e / c.ex) % c.ey), k = (int)(e / ((long long)c.ex * c.ey));
+  const float *V = v + (long long)ev * 3 * c.G;
+  float ax = 0.f, ay = 0.f, az = 0.f;
+  for (int n = lane; n < 125; n += 32) {
+    const int in = n % 5, jn = (n / 5) % 5, kn = n / 25;
+    const long long g = (long long)(i * 4 + in) + (long long)c.GX * ((j * 4 + jn) + (long long)c.GY * (k * 4 + kn));
+    const float w = rec_w[(long long)r * 125 + n];
+    ax = fmaf(V[g], w, ax); ay = fmaf(V[c.G + g], w, ay); az = fmaf(V[2 * c.G + g], w, az);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ax += __shfl_xor_sync(0xffffffffu, ax, o);
+    ay += __shfl_xor_sync(0xffffffffu, ay, o);
+    az += __shfl_xor_sync(0xffffffffu, az, o);
+  }
+  if (lane == 0 && it <= c.nt) {
+    seis[((long long)0 * c.nt + (it - 1)) * R + r] = ax;
+    seis[((long long)1 * c.nt + (it - 1)) * R + r] = ay;
+    seis[((long long)2 * c.nt + (it - 1)) * R + r] = az;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// k_inject: point forces into the element forces, one CTA per (event, element) group,
+// sources of a group applied in file order (ses3d_miscellaneous.f90:33-90).
+// group = {event, element, first source, end source}; stf = [source][3][nt]; mask bit c
+// selects the components a source drives (single force: one; adjoint source: all three).
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_inject(const Consts c, float *__restrict__ f, const int4 *__restrict__ groups,
+                                                const float *__restrict__ delta, const float *__restrict__ stf,
+                                                const int *__restrict__ mask, const int *__restrict__ d_it) {
+  const int4 gr = groups[blockIdx.x];
+  const int n = threadIdx.x;
+  if (n >= 125) return;
+  const int it = *d_it + 1;
+  const long long N = c.N;
+  float *F = f + (long long)gr.x * 3 * N + (long long)gr.y * 125 + n;
+  float fx = F[0], fy = F[N], fz = F[2 * N];
+  for (int s = gr.z; s < gr.w; ++s) {
+    const float d = delta[(long long)s * 125 + n];
+    const float *S = stf + (long long)s * 3 * c.nt + (it - 1);
+    const int m = mask[s];
+    if (m & 1) fx = fx - d * S[0];
+    if (m & 2) fy = fy - d * S[c.nt];
+    if (m & 4) fz = fz - d * S[2 * c.nt];
+  }
+  F[0] = fx; F[N] = fy; F[2 * N] = fz;
+}
+
+// ---------------------------------------------------------------------------------------
+// Layout conversion between the reference layout (element fastest: idx = e + E n) and
+// the internal element-major layout (idx = e*125 + n): 32x32 tiled transpose.
+// in is rows x cols row-major, out is cols x rows row-major.
+// ---------------------------------------------------------------------------------------
+__global__ void k_transpose(const float *__restrict__ in, float *__restrict__ out, long long rows, long long cols) {
+  __shared__ float tile[32][33];
+  const long long c0 = (long long)blockIdx.x * 32, r0 = (long long)blockIdx.y * 32;
+  for (int t = threadIdx.y; t < 32; t += blockDim.y) {
+    const long long rr = r0 + t, cc = c0 + threadIdx.x;
+    if (rr < rows && cc < cols) tile[t][threadIdx.x] = in[rr * cols + cc];
+  }
+  __syncthreads();
+  for (int t = threadIdx.y; t < 32; t += blockDim.y) {
+    const long long cc = c0 + t, rr = r0 + threadIdx.x;
+    if (rr < rows && cc < cols) out[cc * rows + rr] = tile[threadIdx.x][t];
+  }
+}
+
+__global__ void k_transpose_d(const double *__restrict__ in, double *__restrict__ out, long long rows, long long cols) {
+  __shared__ double tile[32][33];
+  const long long c0 = (long long)blockIdx.x * 32, r0 = (long long)blockIdx.y * 32;
+  for (int t = threadIdx.y; t < 32; t += blockDim.y) {
+    const long long rr = r0 + t, cc = c0 + threadIdx.x;
+    if (rr < rows && cc < cols) tile[t][threadIdx.x] = in[rr * cols + cc];
+  }
+  __syncthreads();
+  for (int t = threadIdx.y; t < 32; t += blockDim.y) {
+    const long long cc = c0 + t, rr = r0 + threadIdx.x;
+    if (rr < rows && cc < cols) out[cc * rows + rr] = tile[threadIdx.x][t];
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Model derivation (reference layout, elementwise; SOURCE/ses3d_input.f90:499,
+// SOURCE/ses3d_init.f90:47-61). Rounding follows the reference (no contraction).
+// raw = {rhoinv, mu, lambda, A, B, C, Q} (7 x N), out mat (NMAT x N), gm (NGMAT x N).
+// ---------------------------------------------------------------------------------------
+__global__ void k_derive(const float *__restrict__ raw, float *__restrict__ mat, float *__restrict__ gm, long long N,
+                         int is_diss, float sum_D_p) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= N) return;
+  const float rhoinv = raw[q], mu = raw[N + q], lam = raw[2 * N + q];
+  const float A = raw[3 * N + q], B = raw[4 * N + q], C = raw[5 * N + q];
+  const float kappa = __fadd_rn(lam, __fdiv_rn(__fmul_rn(2.f, mu), 3.f));
+  float tau = 0.f, QQ = 0.f, mu_tau = 0.f;
+  if (is_diss) {
+    QQ = raw[6 * N + q];
+    tau = __fdiv_rn(1.f, QQ);
+    mu_tau = __fmul_rn(__fadd_rn(1.f, __fmul_rn(sum_D_p, tau)), mu);
+    mat[M_CLAM * N + q] = __fsub_rn(kappa, __fdiv_rn(__fmul_rn(2.f, mu_tau), 3.f));
+    mat[M_C2MUT * N + q] = __fmul_rn(2.f, mu_tau);
+    mat[M_C2MT * N + q] = __fmul_rn(__fmul_rn(2.f, mu), tau);
+  } else {
+    mat[M_CLAM * N + q] = lam;
+    mat[M_C2MUT * N + q] = __fmul_rn(2.f, mu);
+    mat[M_C2MT * N + q] = 0.f;
+  }
+  mat[M_A * N + q] = A;
+  mat[M_B2 * N + q] = __fmul_rn(2.f, B);
+  mat[M_C * N + q] = C;
+  if (gm) {
+    gm[G_CS * N + q] = sqrtf(__fmul_rn(mu, rhoinv));
+    gm[G_CP * N + q] = sqrtf(__fmul_rn(__fadd_rn(lam, __fmul_rn(2.f, mu)), rhoinv));
+    gm[G_RHO * N + q] = rhoinv > 0.f ? __fdiv_rn(1.f, rhoinv) : 0.f;
+    gm[G_MU * N + q] = mu;
+    gm[G_KAPPA * N + q] = kappa;
+    gm[G_QQ * N + q] = QQ;
+  }
+}
+
+// Mass matrix (SOURCE/ses3d_init.f90:254-279): each global node sums its element
+// contributions in the reference loop order with IEEE round-to-nearest products, so
+// the result is bit-identical to the reference's FP32 MM_global. rhoinv in reference layout.
+__global__ void k_mass(const Consts c, const float *__restrict__ rhoinv, const float *__restrict__ z,
+                       const float *__restrict__ sinx, const float *__restrict__ w, float Jac, float *__restrict__ MM) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= c.G) return;
+  const int gx = (int)(g % c.GX);
+  const int gy = (int)((g / c.GX) % c.GY);
+  const int gz = (int)(g / ((long long)c.GX * c.GY));
+  const int i0 = gx == 0 ? 0 : (gx - 1) >> 2, i1 = min(gx >> 2, c.ex - 1);
+  const int j0 = gy == 0 ? 0 : (gy - 1) >> 2, j1 = min(gy >> 2, c.ey - 1);
+  const int k0 = gz == 0 ? 0 : (gz - 1) >> 2, k1 = min(gz >> 2, c.ez - 1);
+  float mm = 0.f;
+  for (int i = i0; i <= i1; ++i)
+    for (int j = j0; j <= j1; ++j)
+      for (int k = k0; k <= k1; ++k) {
+        const int l = gx - 4 * i, m = gy - 4 * j, n = gz - 4 * k;
+        const long long e = (long long)i + (long long)c.ex * (j + (long long)c.ey * k);
+        const long long q = e + c.E * (l + 5 * (m + 5 * n));
+        const float zz = z[k * 5 + n];
+        float t = __fmul_rn(__fmul_rn(w[l], w[m]), w[n]);
+        t = __fmul_rn(t, Jac);
+        t = __fmul_rn(t, zz);
+        t = __fmul_rn(t, zz);
+        t = __fmul_rn(t, sinx[i * 5 + l]);
+        t = __fdiv_rn(t, rhoinv[q]);
+        mm = __fsub_rn(mm, t);
+      }
+  MM[g] = mm;
+}
+
+// Max |v| per event (NaN-aware watchdog). out: [nev] as float bits, non-negative.
+__global__ void k_vmax(const float *__restrict__ v, long long G3, unsigned int *__restrict__ out) {
+  const int ev = blockIdx.y;
+  float m = 0.f;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < G3; q += (long long)gridDim.x * blockDim.x) {
+    const float a = fabsf(v[(long long)ev * G3 + q]);
+    m = (a != a) ? __int_as_float(0x7f800000) : fmaxf(m, a);
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out + ev, __float_as_uint(m));
+}
+
+// Normalisation of the Q kernels after the last iteration (ses3d_grad_Q.f90:151-158).
+__global__ void k_grad_q_norm(const Consts c, const float *__restrict__ gm, double *__restrict__ grad) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int ev = blockIdx.y;
+  if (q >= c.N) return;
+  const long long N = c.N;
+  double *G = grad + (long long)ev * NGRAD * N + q;
+  const double mu = gm[G_MU * N + q], kappa = gm[G_KAPPA * N + q], QQ = gm[G_QQ * N + q];
+  const double alpha = 0.3, Q_kappa = 57823.0;
+  G[4 * N] = 2.0 * mu * G[4 * N] / QQ;
+  G[5 * N] = -2.0 * alpha * mu * G[5 * N] / QQ;
+  G[6 * N] = kappa * G[6 * N] / Q_kappa;
+  G[5 * N] = -alpha * kappa * G[7 * N] / Q_kappa;  // the reference overwrites grad_alpha_mu here
+}
+
+// ---------------------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------------------
+template <bool DISS, int MODE, int EPB>
+static cudaError_t launch_elem(const Consts &c, const Ptrs &p, cudaStream_t st) {
+  const long long blocks = (c.E * c.nev + EPB - 1) / EPB;
+  k_element<DISS, MODE, EPB><<<(unsigned)blocks, TPE * EPB, 0, st>>>(c, p);
+  return cudaGetLastError();
+}
+
+template <bool DISS, int MODE>
+static cudaError_t launch_elem_epb(int epb, const Consts &c, const Ptrs &p, cudaStream_t st) {
+  switch (epb) {
+    case 2: return launch_elem<DISS, MODE, 2>(c, p, st);
+    case 4: return launch_elem<DISS, MODE, 4>(c, p, st);
+    default: return launch_elem<DISS, MODE, 1>(c, p, st);
+  }
+}
+
+cudaError_t launch_element(int diss, int mode, int epb, const Consts &c, const Ptrs &p, cudaStream_t st) {
+  if (diss) {
+    if (mode == 1) return launch_elem_epb<true, 1>(epb, c, p, st);
+    if (mode == 2) return launch_elem_epb<true, 2>(epb, c, p, st);
+    return launch_elem_epb<true, 0>(epb, c, p, st);
+  }
+  if (mode == 1) return launch_elem_epb<false, 1>(epb, c, p, st);
+  if (mode == 2) return launch_elem_epb<false, 2>(epb, c, p, st);
+  return launch_elem_epb<false, 0>(epb, c, p, st);
+}
+
+cudaError_t launch_node(const Consts &c, const Ptrs &p, cudaStream_t st) {
+  dim3 grid((unsigned)((c.G + 255) / 256), (unsigned)c.nev);
+  k_node<<<grid, 256, 0, st>>>(c, p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_receivers(const Consts &c, const float *v, const int *rec_elem, const int *rec_ev,
+                             const float *rec_w, float *seis, int R, const int *d_it, cudaStream_t st) {
+  if (R <= 0) return cudaSuccess;
+  k_receivers<<<(R + 3) / 4, 128, 0, st>>>(c, v, rec_elem, rec_ev, rec_w, seis, R, d_it);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_inject(const Consts &c, float *f, const int4 *groups, int ngroups, const float *delta,
+                          const float *stf, const int *mask, const int *d_it, cudaStream_t st) {
+  if (ngroups <= 0) return cudaSuccess;
+  k_inject<<<ngroups, 128, 0, st>>>(c, f, groups, delta, stf, mask, d_it);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_transpose(const float *in, float *out, long long rows, long long cols, cudaStream_t st) {
+  dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+  k_transpose<<<grid, dim3(32, 8), 0, st>>>(in, out, rows, cols);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_transpose_d(const double *in, double *out, long long rows, long long cols, cudaStream_t st) {
+  dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+  k_transpose_d<<<grid, dim3(32, 8), 0, st>>>(in, out, rows, cols);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_derive(const float *raw, float *mat, float *gm, long long N, int is_diss, float sum_D_p,
+                          cudaStream_t st) {
+  k_derive<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(raw, mat, gm, N, is_diss, sum_D_p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mass(const Consts &c, const float *rhoinv, const float *z, const float *sinx, const float *w,
+                        float Jac, float *MM, cudaStream_t st) {
+  k_mass<<<(unsigned)((c.G + 255) / 256), 256, 0, st>>>(c, rhoinv, z, sinx, w, Jac, MM);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vmax(const float *v, long long G3, int nev, unsigned int *out, cudaStream_t st) {
+  dim3 grid(304, (unsigned)nev);
+  k_vmax<<<grid, 256, 0, st>>>(v, G3, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grad_q_norm(const Consts &c, const float *gm, double *grad, cudaStream_t st) {
+  dim3 grid((unsigned)((c.N + 255) / 256), (unsigned)c.nev);
+  k_grad_q_norm<<<grid, 256, 0, st>>>(c, gm, grad);
+  return cudaGetLastError();
+}
+
+// Local (gathered) form of a global field in the reference layout (ses3d_evolution.f90:27-51).
+__global__ void k_gather_ref(const Consts c, const float *__restrict__ v, float *__restrict__ out) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= c.N) return;
+  const long long e = q % c.E;
+  const int n = (int)(q / c.E);
+  const int in = n % 5, jn = (n / 5) % 5, kn = n / 25;
+  const int i = (int)(e % c.ex), j = (int)((e / c.ex) % c.ey), k = (int)(e / ((long long)c.ex * c.ey));
+  out[q] = v[(long long)(i * 4 + in) + (long long)c.GX * ((j * 4 + jn) + (long long)c.GY * (k * 4 + kn))];
+}
+
+cudaError_t launch_gather_ref(const Consts &c, const float *v, float *out, cudaStream_t st) {
+  k_gather_ref<<<(unsigned)((c.N + 255) / 256), 256, 0, st>>>(c, v, out);
+  return cudaGetLastError();
+}
+
+}  // namespace ses3d

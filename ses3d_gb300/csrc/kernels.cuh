@@ -1,0 +1,72 @@
+// kernels.cuh -- device data structures shared by the SES3D kernels and the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ses3d {
+
+constexpr int TPE = 128;  // threads per element (125 GLL nodes + 3 idle lanes)
+
+// Element-local state, per event: 36 SoA fields of N floats, element-major
+// ([element][125 nodes], node n = in + 5 jn + 25 kn).
+enum StateField {
+  F_SXX = 0, F_SYY, F_SZZ, F_SXY, F_SYX, F_SXZ, F_SZX, F_SYZ, F_SZY,        // PML-split stresses
+  F_DXUX = 9, F_DYUY, F_DZUZ, F_DXUY, F_DYUX, F_DXUZ, F_DZUX, F_DYUZ, F_DZUY, // displacement gradients
+  F_M = 18,  // memory variables: F_M + 3*comp + mech, comp = xx, yy, zz, xy, xz, yz
+  NSTATE = 36
+};
+
+// Per-node material coefficients (element-major), derived once from the model.
+enum MatField { M_CLAM = 0, M_C2MUT, M_C2MT, M_A, M_B2, M_C, NMAT };
+// Adjoint-only per-node quantities.
+enum GMatField { G_RHO = 0, G_CP, G_CS, G_MU, G_KAPPA, G_QQ, NGMAT };
+// Forward record fields (the ffd files of the reference).
+enum RecField { R_VX = 0, R_VY, R_VZ, R_EXX, R_EYY, R_EZZ, R_EXY, R_EXZ, R_EYZ, NREC };
+constexpr int NGRAD = 8;  // rho, cp, csh, csv, Q_mu, alpha_mu, Q_kappa, alpha_kappa
+
+// Small per-mesh coefficient tables, copied into shared memory by each CTA.
+struct KTab {
+  float Dx[5][5], Dy[5][5], Dz[5][5];  // strain: D[i][q] = 2 dl(q,i) / d   (ses3d_evolution.f90:66-68)
+  float dlT[5][5];                     // divergence: dl(i,q)               (ses3d_evolution.f90:247-249)
+  float CX[5][5], CY[5][5], CZ[5][5];  // (2/dx)Jac w_j w_k, (2/dy)Jac w_i w_k, -(2/dz)Jac w_i w_j
+  float w[5];
+};
+constexpr int KTAB_FLOATS = sizeof(KTab) / sizeof(float);
+
+struct Consts {
+  int ex, ey, ez, nev, nt;
+  int GX, GY, GZ;
+  long long E, N, G;
+  float dt;
+  float a_k[3];   // dt / tau_p(k)
+  float L_k[3];   // dt * D_p(k) / tau_p(k)
+  float s_grad;   // samp_ad * dt
+  float inv_jac;  // unused by the reference-order path; kept for the Q kernels
+  float Jac;
+  float tau_p[3], D_p[3];
+};
+
+struct Ptrs {
+  const KTab *ktab;
+  const float *sin_x, *cot_x, *r_z;     // [i*5+n], [k*5+n]
+  const float *pxr, *pyr, *pzr;         // raw PML per element node
+  const float *pxg, *pyg, *pzg;         // raw PML per global index (last writer)
+  const float *MM;                      // [G]
+  const float *mat;                     // [NMAT][N]
+  const float *gmat;                    // [NGMAT][N] (adjoint)
+  float *state;                         // [nev][NSTATE][N]
+  float *v;                             // [nev][3][G]
+  float *f;                             // [nev][3][N] element-local forces (scratch)
+  int *d_it;                            // completed iterations
+  // moment-tensor source per event
+  const int *src_elem;                  // [nev], -1: none
+  const float *src_delta;               // [nev][125]
+  const float *src_mom;                 // [nev][6]
+  const float *stf;                     // [nev][nt]
+  // forward records / kernels
+  float *rec;                           // record of this iteration: [nev][NREC][N]
+  double *grad;                         // [nev][NGRAD][N]
+  int grad_q;                           // accumulate the Q kernels too
+};
+
+}  // namespace ses3d

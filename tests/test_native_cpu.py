@@ -1,0 +1,60 @@
+"""CPU checks of the native boundary: the library builds, loads, and exports every
+entry point include/ses3d_gpu.h declares; without a GPU it fails cleanly."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    with open(os.path.join(ROOT, "include", "ses3d_gpu.h")) as f:
+        txt = f.read()
+    return sorted(set(re.findall(r"\b(ses3d_gpu_\w+)\s*\(", txt)))
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert "ses3d_gpu_create" in syms and "ses3d_gpu_step" in syms
+    assert len(syms) >= 30
+
+
+def test_library_exports_every_declared_symbol(native):
+    lib = ctypes.CDLL(os.path.join(ROOT, "ses3d_gb300", "libses3d_gpu.so"))
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_binding_covers_header(native):
+    from ses3d_gb300 import _lib
+    assert set(declared_symbols()) <= set(_lib.SIGNATURES), set(declared_symbols()) - set(_lib.SIGNATURES)
+
+
+def test_version_string(native):
+    assert b"sm_103a" in native.ses3d_gpu_version()
+
+
+def test_create_without_gpu_fails_cleanly(native):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from ses3d_gb300 import _lib
+    from ses3d_gb300 import synth
+    from ses3d_gb300.solver import Simulation, config_from
+    p = synth.make_problem("tiny", nt=5, model=False)
+    cfg = config_from(p.box, p.setup, 5, p.events[0].event.dt, p.tau, p.D, pml=3)
+    with pytest.raises(_lib.Ses3dError) as ei:
+        Simulation(cfg)
+    assert ei.value.code == -7
+
+
+def test_create_rejects_bad_config(native):
+    from ses3d_gb300 import _lib
+    cfg = _lib.Config()
+    cfg.lpd = 5
+    h = ctypes.c_void_p()
+    rc = native.ses3d_gpu_create(ctypes.byref(cfg), ctypes.byref(h))
+    assert rc == -1
+    assert b"lpd" in native.ses3d_gpu_last_error(None)
