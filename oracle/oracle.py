@@ -204,5 +204,5 @@ class Oracle:
         return out.reshape(9, n)
 
     def set_records(self, recs: np.ndarray):
-        a = np.ascontiguousarray(recs, np.float32)
+        a = np.ascontiguousarray(recs, self.dtype)
         self.lib.oracle_set_records(self.h, a.shape[0], a.ctypes.data_as(ctypes.c_void_p))

@@ -1011,7 +1011,8 @@ template <class T> struct Sim : Base {
     return 0;
   }
   int set_records(int nrec, const void *data) override {
-    const float *p = (const float *)data;  // records are always FP32 on disk
+    // records in the handle's precision (FP32 as on disk; FP64 for the -fdefault-real-8 stand-in)
+    const T *p = (const T *)data;
     records.assign(nrec, V(9 * N));
     for (int r = 0; r < nrec; ++r)
       for (long q = 0; q < 9 * N; ++q) records[r][q] = (T)p[(size_t)r * 9 * N + q];

@@ -1,0 +1,112 @@
+"""GPU parity of the adjoint path: forward-field records (adjoint_flag 1) and Frechet
+kernels (adjoint_flag 2, SOURCE/ses3d_grad.f90 and SOURCE/ses3d_grad_Q.f90) against the
+CPU oracle. Kernel tolerance: rel-L2 <= 1e-3 against the FP64 oracle."""
+import numpy as np
+import pytest
+
+from ses3d_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+NT = 60
+SAMP = 5
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def adjoint_inputs(p, seis):
+    """Two adjoint sources at the first two receivers, driven by the time-reversed forward
+    velocity (the shape TOOLS/adjoint_source.py writes for a waveform misfit)."""
+    loc = p.events[0].receivers.loc[:2].copy()
+    loc[:, 2] = np.float32(1000.0)  # 1 km depth, as in ADJOINT/1/ad_srcfile of the reference
+    stf = np.zeros((2, 3, NT), np.float32)
+    for k in range(2):
+        for c in range(3):
+            stf[k, c] = seis[c][k][::-1]
+    stf *= np.float32(1e10) / np.abs(stf).max()
+    return loc, stf
+
+
+@pytest.fixture(scope="module")
+def problem():
+    p = synth.make_problem("small", nt=NT, seed=31, adjoint_flag=1)
+    p.setup.samp_ad = SAMP
+    return p
+
+
+@pytest.fixture(scope="module")
+def runs(native, oracle_mod, problem):
+    from ses3d_gb300.solver import Simulation
+    p = problem
+    out = {}
+    sim = Simulation.from_problem(p, adjoint_flag=1, grad_variant=1)
+    sim.run()
+    out["gpu_records"] = [sim.record(r) for r in range(sim.record_count())]
+    out["gpu_sv"] = sim.saving_vector()
+    gseis = sim.seismograms(0)
+    loc, stf = adjoint_inputs(p, gseis)
+    out["nad"] = sim.set_adjoint_sources(0, loc, stf)
+    sim.begin_adjoint()
+    sim.run()
+    out["gpu_kernels"] = {k: sim.kernel(k) for k in ("rho", "cp", "csh", "csv", "Q_mu", "alpha_mu", "Q_kappa")}
+    out["gpu_is"] = sim.setup_int("is")
+    sim.close()
+    for fp64 in (False, True):
+        o = oracle_mod.Oracle(p, fp64=fp64, adjoint_flag=1)
+        o.run(NT)
+        recs = np.stack([o.record(r) for r in range(o.nrecords())])
+        sv = o.get_int("saving_vector")[1:NT + 1]
+        oa = oracle_mod.Oracle(p, fp64=fp64, adjoint_flag=2, saving_vector=sv, ad_loc=loc, ad_stf=stf,
+                               grad_variant=1)
+        oa.set_records(recs)
+        oa.run(NT)
+        tag = "64" if fp64 else "32"
+        out["o_records" + tag] = recs
+        out["o_sv" + tag] = sv
+        out["o_kernels" + tag] = {k: oa.get("grad_" + k) for k in ("rho", "cp", "csh", "csv", "Q_mu",
+                                                                   "alpha_mu", "Q_kappa")}
+        out["o_is" + tag] = oa.get_int("is")
+        out["o_nad" + tag] = int(oa.get_int("nr_adsrc")[0])
+    return out
+
+
+def test_saving_vector(runs):
+    assert np.array_equal(runs["gpu_sv"], runs["o_sv32"])
+    expected = [it if (it % SAMP == 0 or it == 1 or it == NT) else 0 for it in range(1, NT + 1)]
+    assert list(runs["gpu_sv"]) == expected
+
+
+def test_records(runs):
+    g, o = runs["gpu_records"], runs["o_records64"]
+    assert len(g) == len(o)
+    for r in range(len(g)):
+        for f in range(9):
+            if np.abs(o[r][f]).max() == 0:
+                assert np.abs(g[r][f]).max() == 0
+                continue
+            assert rel(g[r][f], o[r][f]) <= 1e-4, (r, f, rel(g[r][f], o[r][f]))
+
+
+def test_adjoint_source_location_bit_exact(runs):
+    assert runs["nad"] == runs["o_nad32"] == 2
+    assert np.array_equal(runs["gpu_is"], runs["o_is32"][: 3 * runs["nad"]])
+
+
+@pytest.mark.parametrize("name", ["rho", "cp", "csh", "csv"])
+def test_kernels(runs, name):
+    g = runs["gpu_kernels"][name]
+    o64 = runs["o_kernels64"][name]
+    o32 = runs["o_kernels32"][name]
+    assert np.abs(o64).max() > 0
+    assert rel(g, o64) <= 1e-3, (name, rel(g, o64), rel(o32, o64))
+
+
+@pytest.mark.parametrize("name", ["Q_mu", "alpha_mu", "Q_kappa"])
+def test_q_kernels(runs, name):
+    g = runs["gpu_kernels"][name]
+    o64 = runs["o_kernels64"][name]
+    assert np.abs(o64).max() > 0
+    assert rel(g, o64) <= 1e-3, (name, rel(g, o64))
