@@ -85,6 +85,7 @@ struct ses3d_gpu {
   std::vector<int> saving_vector;  // [nt+1]
   std::vector<EventHost> ev;
   // tables offsets
+  size_t o_isin = 0, o_ir = 0;
   size_t o_sin = 0, o_cot = 0, o_r = 0, o_pxr = 0, o_pyr = 0, o_pzr = 0, o_pxg = 0, o_pyg = 0, o_pzg = 0, o_z = 0,
          o_w = 0;
   // per-kernel timing
@@ -133,6 +134,7 @@ Ptrs make_ptrs(ses3d_gpu *h) {
   std::memset(&p, 0, sizeof(p));
   p.ktab = h->d_ktab;
   p.sin_x = h->d_tab + h->o_sin; p.cot_x = h->d_tab + h->o_cot; p.r_z = h->d_tab + h->o_r;
+  p.inv_sin = h->d_tab + h->o_isin; p.inv_r = h->d_tab + h->o_ir;
   p.pxr = h->d_tab + h->o_pxr; p.pyr = h->d_tab + h->o_pyr; p.pzr = h->d_tab + h->o_pzr;
   p.pxg = h->d_tab + h->o_pxg; p.pyg = h->d_tab + h->o_pyg; p.pzg = h->d_tab + h->o_pzg;
   p.MM = h->d_MM; p.mat = h->d_mat; p.gmat = h->d_gmat;
@@ -453,6 +455,11 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   put(h->o_pxg, g.pxg); put(h->o_pyg, g.pyg); put(h->o_pzg, g.pzg);
   put(h->o_z, g.z);
   put(h->o_w, std::vector<float>(g.w, g.w + NP));
+  std::vector<float> isin(g.sin_x.size()), ir(g.z.size());
+  for (size_t q = 0; q < isin.size(); ++q) isin[q] = 1.0f / g.sin_x[q];
+  for (size_t q = 0; q < ir.size(); ++q) ir[q] = 1.0f / g.z[q];
+  put(h->o_isin, isin);
+  put(h->o_ir, ir);
   const size_t nev = cfg->n_events;
   cudaError_t e = cudaSuccess;
   auto chk = [&](cudaError_t x) { if (x != cudaSuccess && e == cudaSuccess) e = x; };

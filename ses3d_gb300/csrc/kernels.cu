@@ -13,14 +13,21 @@
 // contributions in the reference loop order, without atomics, so runs are bit-reproducible.
 #include "kernels.cuh"
 
+// Minimum resident CTAs per SM requested from ptxas for k_element (register cap).
+#ifndef SES3D_ELEM_MINB
+#define SES3D_ELEM_MINB 6
+#endif
+
 namespace ses3d {
 
 // ---------------------------------------------------------------------------------------
-// k_element: one element per 128 threads (thread = GLL node), EPB elements per CTA.
-// MODE 0 plain, 1 store forward record, 2 adjoint with kernel correlation.
+// k_element: one element per 128 threads (thread = GLL node), EPB consecutive x-elements
+// per CTA; grid (ceil(ex/EPB), ey, ez * n_events). MODE 0 plain, 1 store forward record,
+// 2 adjoint with kernel correlation. Every independent global load (state, material, v)
+// is issued before the first barrier so that a thread has all its bytes in flight at once.
 // ---------------------------------------------------------------------------------------
 template <bool DISS, int MODE, int EPB>
-__global__ void __launch_bounds__(TPE * EPB) k_element(const Consts c, const Ptrs p) {
+__global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_ELEM_MINB / EPB : 1)) k_element(const Consts c, const Ptrs p) {
   __shared__ KTab tab;
   __shared__ float s_v[EPB][3][TPE];
   __shared__ float s_p[EPB][9][TPE];
@@ -30,33 +37,41 @@ __global__ void __launch_bounds__(TPE * EPB) k_element(const Consts c, const Ptr
 
   const int sub = threadIdx.x / TPE;
   const int n = threadIdx.x % TPE;
-  const long long blk = (long long)blockIdx.x * EPB + sub;
-  const bool blk_ok = blk < c.E * c.nev;
-  const int ev = blk_ok ? (int)(blk % c.nev) : 0;
-  const long long e = blk_ok ? blk / c.nev : 0;
-  const bool act = blk_ok && n < 125;
+  const int i = blockIdx.x * EPB + sub;
+  const int j = blockIdx.y;
+  const int k = (int)blockIdx.z / c.nev;
+  const int ev = (int)blockIdx.z - k * c.nev;
+  const bool act = i < c.ex && n < 125;
   const int nn = act ? n : 0;
+  const int ii = act ? i : 0;
   const int in = nn % 5, jn = (nn / 5) % 5, kn = nn / 25;
-  const int i = (int)(e % c.ex);
-  const int j = (int)((e / c.ex) % c.ey);
-  const int k = (int)(e / ((long long)c.ex * c.ey));
-  const long long N = c.N;
+  const unsigned e = (unsigned)ii + (unsigned)c.ex * ((unsigned)j + (unsigned)c.ey * (unsigned)k);
+  const size_t N = (size_t)c.N;
+  const size_t m0 = (size_t)e * 125 + nn;  // material / element-local index
+  float *S = p.state + (size_t)ev * NSTATE * N + m0;
+  const float *MT = p.mat + m0;
 
-  // gather v_global -> element-local v (ses3d_evolution.f90:27-51)
+  constexpr int NS = DISS ? NSTATE : 18;  // elastic runs carry no memory variables
+  float sv[NS];
+  float clam = 0.f, c2mut = 0.f, c2mt = 0.f, cA = 0.f, cB2 = 0.f, cC = 0.f;
   float vx = 0.f, vy = 0.f, vz = 0.f;
   if (act) {
-    const long long g = (long long)(i * 4 + in) + (long long)c.GX * ((j * 4 + jn) + (long long)c.GY * (k * 4 + kn));
-    const float *v = p.v + (long long)ev * 3 * c.G;
-    vx = v[g]; vy = v[c.G + g]; vz = v[2 * c.G + g];
+    // gather v_global -> element-local v (ses3d_evolution.f90:27-51)
+    const size_t g = (size_t)(ii * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
+    const float *v = p.v + (size_t)ev * 3 * c.G + g;
+    vx = v[0]; vy = v[c.G]; vz = v[2 * c.G];
+#pragma unroll
+    for (int f = 0; f < NS; ++f) sv[f] = S[f * N];
+    clam = __ldg(MT + M_CLAM * N); c2mut = __ldg(MT + M_C2MUT * N);
+    if (DISS) c2mt = __ldg(MT + M_C2MT * N);
+    cA = __ldg(MT + M_A * N); cB2 = __ldg(MT + M_B2 * N); cC = __ldg(MT + M_C * N);
+  } else {
+#pragma unroll
+    for (int f = 0; f < NS; ++f) sv[f] = 0.f;
   }
   s_v[sub][0][n] = vx; s_v[sub][1][n] = vy; s_v[sub][2][n] = vz;
   __syncthreads();
 
-  const long long q0 = (long long)ev * NSTATE * N + e * 125 + nn;  // state field 0 of this node
-  float *S = p.state + q0;
-  const long long m0 = e * 125 + nn;  // material / element-local index
-
-  float fx = 0.f, fy = 0.f, fz = 0.f;
   float r = 1.f, st = 1.f;
   if (act) {
     // strain-rate proxies (ses3d_evolution.f90:57-87)
@@ -75,31 +90,33 @@ __global__ void __launch_bounds__(TPE * EPB) k_element(const Consts c, const Ptr
       ezy = fmaf(s_v[sub][1][iz], dzq, ezy);
       ezz = fmaf(s_v[sub][2][iz], dzq, ezz);
     }
-    // spherical completion (ses3d_evolution.f90:93-103)
+    // spherical completion (ses3d_evolution.f90:93-103), divisions by r and r sin(theta)
+    // taken as products with the tabulated reciprocals
     r = __ldg(p.r_z + k * 5 + kn);
-    st = __ldg(p.sin_x + i * 5 + in);
-    const float ct = __ldg(p.cot_x + i * 5 + in);
-    const float rs = r * st;
+    st = __ldg(p.sin_x + ii * 5 + in);
+    const float ir = __ldg(p.inv_r + k * 5 + kn);
+    const float irs = ir * __ldg(p.inv_sin + ii * 5 + in);
+    const float ct = __ldg(p.cot_x + ii * 5 + in);
     ezz = -ezz;
-    eyy = eyy / rs + (vz + vx * ct) / r;
-    exx = (vz + exx) / r;
+    eyy = eyy * irs + (vz + vx * ct) * ir;
+    exx = (vz + exx) * ir;
     ezx = -ezx;
-    exz = (exz - vx) / r;
+    exz = (exz - vx) * ir;
     ezy = -ezy;
-    eyz = -vy / r + eyz / rs;
-    exy = exy / r;
-    eyx = -vy * ct / r + eyx / rs;
+    eyz = -vy * ir + eyz * irs;
+    exy = exy * ir;
+    eyx = -vy * ct * ir + eyx * irs;
     // displacement gradients (ses3d_evolution.f90:109-117)
     const float dt = c.dt;
-    const float dxux = S[F_DXUX * N] + dt * exx, dyuy = S[F_DYUY * N] + dt * eyy, dzuz = S[F_DZUZ * N] + dt * ezz;
-    const float dxuy = S[F_DXUY * N] + dt * exy, dyux = S[F_DYUX * N] + dt * eyx;
-    const float dxuz = S[F_DXUZ * N] + dt * exz, dzux = S[F_DZUX * N] + dt * ezx;
-    const float dyuz = S[F_DYUZ * N] + dt * eyz, dzuy = S[F_DZUY * N] + dt * ezy;
+    const float dxux = sv[F_DXUX] + dt * exx, dyuy = sv[F_DYUY] + dt * eyy, dzuz = sv[F_DZUZ] + dt * ezz;
+    const float dxuy = sv[F_DXUY] + dt * exy, dyux = sv[F_DYUX] + dt * eyx;
+    const float dxuz = sv[F_DXUZ] + dt * exz, dzux = sv[F_DZUX] + dt * ezx;
+    const float dyuz = sv[F_DYUZ] + dt * eyz, dzuy = sv[F_DZUY] + dt * ezy;
     S[F_DXUX * N] = dxux; S[F_DYUY * N] = dyuy; S[F_DZUZ * N] = dzuz;
     S[F_DXUY * N] = dxuy; S[F_DYUX * N] = dyux; S[F_DXUZ * N] = dxuz;
     S[F_DZUX * N] = dzux; S[F_DYUZ * N] = dyuz; S[F_DZUY * N] = dzuy;
     // PML profiles of this node (ses3d_init.f90:678-686), corners normalised
-    const float pxr = __ldg(p.pxr + i * 5 + in), pyr = __ldg(p.pyr + j * 5 + jn), pzr = __ldg(p.pzr + k * 5 + kn);
+    const float pxr = __ldg(p.pxr + ii * 5 + in), pyr = __ldg(p.pyr + j * 5 + jn), pzr = __ldg(p.pzr + k * 5 + kn);
     float px = 0.f, py = 0.f, pz = 0.f, taper = 1.f;
     const float praw = __fadd_rn(__fadd_rn(pxr, pyr), pzr);
     if (praw != 0.f) {
@@ -124,16 +141,12 @@ __global__ void __launch_bounds__(TPE * EPB) k_element(const Consts c, const Ptr
     exz = (exz + ezx) * 0.5f;
     eyz = (eyz + ezy) * 0.5f;
     // stress rates (ses3d_evolution.f90:146-202)
-    const float *MT = p.mat + m0;
-    const float clam = __ldg(MT + M_CLAM * N), c2mut = __ldg(MT + M_C2MUT * N);
-    const float cA = __ldg(MT + M_A * N), cB2 = __ldg(MT + M_B2 * N), cC = __ldg(MT + M_C * N);
     const float tr = exx + eyy + ezz;
     float sxx, syy, szz, sxy, sxz, syz;
     float Mv[18];
     if (DISS) {
-      const float c2mt = __ldg(MT + M_C2MT * N);
 #pragma unroll
-      for (int t = 0; t < 18; ++t) Mv[t] = S[(F_M + t) * N];
+      for (int t = 0; t < 18; ++t) Mv[t] = sv[(F_M + t) % NS];
       const float Mdx = Mv[0] + Mv[1] + Mv[2], Mdy = Mv[3] + Mv[4] + Mv[5], Mdz = Mv[6] + Mv[7] + Mv[8];
       const float Mxy = Mv[9] + Mv[10] + Mv[11], Mxz = Mv[12] + Mv[13] + Mv[14], Myz = Mv[15] + Mv[16] + Mv[17];
       const float Lw = clam * tr - c2mt * (Mdx + Mdy + Mdz) * (1.f / 3.f);
@@ -164,9 +177,9 @@ __global__ void __launch_bounds__(TPE * EPB) k_element(const Consts c, const Ptr
       syz = c2mut * eyz + cB2 * eyz;
     }
     // march PML stresses (ses3d_evolution.f90:208-219)
-    float s_xx = S[F_SXX * N], s_yy = S[F_SYY * N], s_zz = S[F_SZZ * N];
-    float s_xy = S[F_SXY * N], s_yx = S[F_SYX * N], s_xz = S[F_SXZ * N];
-    float s_zx = S[F_SZX * N], s_yz = S[F_SYZ * N], s_zy = S[F_SZY * N];
+    float s_xx = sv[F_SXX], s_yy = sv[F_SYY], s_zz = sv[F_SZZ];
+    float s_xy = sv[F_SXY], s_yx = sv[F_SYX], s_xz = sv[F_SXZ];
+    float s_zx = sv[F_SZX], s_yz = sv[F_SYZ], s_zy = sv[F_SZY];
     s_xx = s_xx + dt * (sxx - px * s_xx);
     s_yy = s_yy + dt * (syy - py * s_yy);
     s_zz = s_zz + dt * (szz - pz * s_zz);
@@ -181,10 +194,10 @@ __global__ void __launch_bounds__(TPE * EPB) k_element(const Consts c, const Ptr
     S[F_SXY * N] = s_xy * taper; S[F_SYX * N] = s_yx * taper; S[F_SXZ * N] = s_xz * taper;
     S[F_SZX * N] = s_zx * taper; S[F_SYZ * N] = s_yz * taper; S[F_SZY * N] = s_zy * taper;
     // moment-tensor source field (ses3d_miscellaneous.f90:115-147)
-    if (MODE != 2 && e == (long long)__ldg(p.src_elem + ev)) {
+    if (MODE != 2 && (int)e == __ldg(p.src_elem + ev)) {
       const int it = *p.d_it + 1;
       const float d = p.src_delta[ev * 125 + nn];
-      const float so = p.stf[(long long)ev * c.nt + (it - 1)];
+      const float so = p.stf[(size_t)ev * c.nt + (it - 1)];
       const float *mom = p.src_mom + ev * 6;
       const float sxxs = -(__fmul_rn(__fmul_rn(mom[0], d), so)), syys = -(__fmul_rn(__fmul_rn(mom[1], d), so));
       const float szzs = -(__fmul_rn(__fmul_rn(mom[2], d), so)), sxys = -(__fmul_rn(__fmul_rn(mom[3], d), so));
@@ -199,13 +212,13 @@ __global__ void __launch_bounds__(TPE * EPB) k_element(const Consts c, const Ptr
     s_p[sub][6][n] = wz * s_zx; s_p[sub][7][n] = wz * s_zy; s_p[sub][8][n] = wz * s_zz;
 
     if (MODE == 1) {  // forward record (ses3d_main.f90:148-158)
-      float *R = p.rec + (long long)ev * NREC * N + m0;
+      float *R = p.rec + (size_t)ev * NREC * N + m0;
       R[R_VX * N] = vx; R[R_VY * N] = vy; R[R_VZ * N] = vz;
       R[R_EXX * N] = dxux; R[R_EYY * N] = dyuy; R[R_EZZ * N] = dzuz;
-      R[R_EXY * N] = (dxuy + dyux) / 2.f; R[R_EXZ * N] = (dxuz + dzux) / 2.f; R[R_EYZ * N] = (dyuz + dzuy) / 2.f;
+      R[R_EXY * N] = (dxuy + dyux) * 0.5f; R[R_EXZ * N] = (dxuz + dzux) * 0.5f; R[R_EYZ * N] = (dyuz + dzuy) * 0.5f;
     }
     if (MODE == 2 && p.rec) {  // kernel correlation (ses3d_grad.f90:53-83, ses3d_grad_Q.f90:111-143)
-      const float *R = p.rec + (long long)ev * NREC * N + m0;
+      const float *R = p.rec + (size_t)ev * NREC * N + m0;
       const float vxf = R[R_VX * N], vyf = R[R_VY * N], vzf = R[R_VZ * N];
       const float exxf = R[R_EXX * N], eyyf = R[R_EYY * N], ezzf = R[R_EZZ * N];
       const float exyf = R[R_EXY * N], exzf = R[R_EXZ * N], eyzf = R[R_EYZ * N];
@@ -217,7 +230,7 @@ __global__ void __launch_bounds__(TPE * EPB) k_element(const Consts c, const Ptr
       const float *GM = p.gmat + m0;
       const float rho = GM[G_RHO * N], cp = GM[G_CP * N], cs = GM[G_CS * N];
       const double sj = (double)c.s_grad / (double)c.Jac;
-      double *GR = p.grad + (long long)ev * NGRAD * N + m0;
+      double *GR = p.grad + (size_t)ev * NGRAD * N + m0;
       GR[0 * N] += sj * (double)((vxf * vx + vyf * vy + vzf * vz) +
                                  ((cp * cp - 2.f * cs * cs) * tr_fw * tr_ad + 2.f * cs * cs * edde));
       GR[1 * N] += sj * (double)(2.f * rho * cp * tr_fw * tr_ad);
@@ -267,38 +280,40 @@ __global__ void __launch_bounds__(TPE * EPB) k_element(const Consts c, const Ptr
       az2 = fmaf(s_p[sub][8][iz], dzq, az2);
     }
     const float cx = tab.CX[jn][kn] * r, cy = tab.CY[in][kn] * r, cz = tab.CZ[in][jn] * st;
-    fx = cx * ax0 + cy * ay0 + cz * az0;
-    fy = cx * ax1 + cy * ay1 + cz * az1;
-    fz = cx * ax2 + cy * ay2 + cz * az2;
-    float *F = p.f + (long long)ev * 3 * N + m0;
-    F[0] = fx; F[N] = fy; F[2 * N] = fz;
+    float *F = p.f + (size_t)ev * 3 * N + m0;
+    F[0] = cx * ax0 + cy * ay0 + cz * az0;
+    F[N] = cx * ax1 + cy * ay1 + cz * az1;
+    F[2 * N] = cx * ax2 + cy * ay2 + cz * az2;
   }
 }
 
 // ---------------------------------------------------------------------------------------
-// k_node: one thread per (global node, event). Deterministic assembly in the reference
-// order (element i, then j, then k ascending; ses3d_evolution.f90:286-310), then
-// a = s / MM, v += dt (a - prof v), v *= taper (ses3d_evolution.f90:318-328,366).
+// k_node: one thread per (global node, event); grid (ceil(GX*GY/256), GZ, n_events).
+// Deterministic assembly in the reference order (element i, then j, then k ascending;
+// ses3d_evolution.f90:286-310), then a = s / MM, v += dt (a - prof v), v *= taper
+// (ses3d_evolution.f90:318-328,366).
 // ---------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_node(const Consts c, const Ptrs p) {
-  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int ev = blockIdx.y;
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *p.d_it += 1;  // all readers finished earlier in stream order
-  if (g >= c.G) return;
-  const int gx = (int)(g % c.GX);
-  const int gy = (int)((g / c.GX) % c.GY);
-  const int gz = (int)(g / ((long long)c.GX * c.GY));
+  const unsigned t = blockIdx.x * 256u + threadIdx.x;
+  const int gz = blockIdx.y, ev = blockIdx.z;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
+    *p.d_it += 1;  // every reader of the counter ran earlier in stream order
+  const unsigned GXY = (unsigned)c.GX * (unsigned)c.GY;
+  if (t >= GXY) return;
+  const int gy = (int)(t / (unsigned)c.GX);
+  const int gx = (int)t - gy * c.GX;
+  const size_t g = (size_t)gz * GXY + t;
   const int i0 = gx == 0 ? 0 : (gx - 1) >> 2, i1 = min(gx >> 2, c.ex - 1);
   const int j0 = gy == 0 ? 0 : (gy - 1) >> 2, j1 = min(gy >> 2, c.ey - 1);
   const int k0 = gz == 0 ? 0 : (gz - 1) >> 2, k1 = min(gz >> 2, c.ez - 1);
-  const long long N = c.N;
-  const float *F = p.f + (long long)ev * 3 * N;
+  const size_t N = (size_t)c.N;
+  const float *F = p.f + (size_t)ev * 3 * N;
   float sx = 0.f, sy = 0.f, sz = 0.f;
   for (int i = i0; i <= i1; ++i)
     for (int j = j0; j <= j1; ++j)
       for (int k = k0; k <= k1; ++k) {
-        const long long q = ((long long)i + (long long)c.ex * (j + (long long)c.ey * k)) * 125 +
-                            (gx - 4 * i) + 5 * (gy - 4 * j) + 25 * (gz - 4 * k);
+        const size_t q = (size_t)((unsigned)i + (unsigned)c.ex * ((unsigned)j + (unsigned)c.ey * (unsigned)k)) * 125 +
+                         (gx - 4 * i) + 5 * (gy - 4 * j) + 25 * (gz - 4 * k);
         sx += F[q]; sy += F[N + q]; sz += F[2 * N + q];
       }
   const float mm = p.MM[g];
@@ -314,7 +329,7 @@ __global__ void __launch_bounds__(256) k_node(const Consts c, const Ptrs p) {
     prof = __fadd_rn(__fadd_rn(px, py), pz);
     taper = expf(-__fmul_rn(__fmul_rn(0.1f, prof), prof));
   }
-  float *V = p.v + (long long)ev * 3 * c.G + g;
+  float *V = p.v + (size_t)ev * 3 * c.G + g;
   const float dt = c.dt;
   float vx = V[0], vy = V[c.G], vz = V[2 * c.G];
   vx = vx + dt * (ax - prof * vx);
@@ -521,8 +536,8 @@ __global__ void k_grad_q_norm(const Consts c, const float *__restrict__ gm, doub
 // ---------------------------------------------------------------------------------------
 template <bool DISS, int MODE, int EPB>
 static cudaError_t launch_elem(const Consts &c, const Ptrs &p, cudaStream_t st) {
-  const long long blocks = (c.E * c.nev + EPB - 1) / EPB;
-  k_element<DISS, MODE, EPB><<<(unsigned)blocks, TPE * EPB, 0, st>>>(c, p);
+  dim3 grid((unsigned)((c.ex + EPB - 1) / EPB), (unsigned)c.ey, (unsigned)(c.ez * c.nev));
+  k_element<DISS, MODE, EPB><<<grid, TPE * EPB, 0, st>>>(c, p);
   return cudaGetLastError();
 }
 
@@ -547,7 +562,7 @@ cudaError_t launch_element(int diss, int mode, int epb, const Consts &c, const P
 }
 
 cudaError_t launch_node(const Consts &c, const Ptrs &p, cudaStream_t st) {
-  dim3 grid((unsigned)((c.G + 255) / 256), (unsigned)c.nev);
+  dim3 grid((unsigned)(((long long)c.GX * c.GY + 255) / 256), (unsigned)c.GZ, (unsigned)c.nev);
   k_node<<<grid, 256, 0, st>>>(c, p);
   return cudaGetLastError();
 }

@@ -49,6 +49,7 @@ struct Consts {
 struct Ptrs {
   const KTab *ktab;
   const float *sin_x, *cot_x, *r_z;     // [i*5+n], [k*5+n]
+  const float *inv_sin, *inv_r;         // reciprocals of sin_x and r_z
   const float *pxr, *pyr, *pzr;         // raw PML per element node
   const float *pxg, *pyg, *pzg;         // raw PML per global index (last writer)
   const float *MM;                      // [G]
