@@ -216,6 +216,33 @@ int ses3d_gpu_use_graph(ses3d_gpu *h, int enable, int n_per_graph);
 int ses3d_gpu_profile(ses3d_gpu *h, int enable);
 int ses3d_gpu_kernel_time(const ses3d_gpu *h, int which, double *total_ms, int64_t *launches);
 
+/* Allocation-free forward iterations, for callers that cannot call cudaMalloc at the
+ * point where they step the solver: code whose device memory belongs to another
+ * allocator (a PyTorch or JAX caching allocator, a pre-sized memory pool) or that runs
+ * in a loop where allocating is not allowed. It has no counterpart in the reference
+ * (whose arrays are all static Fortran module variables).
+ * The caller owns the wavefield and passes it in device memory:
+ *   state: n_events x 36 x N floats -- per event the element-local fields in the order
+ *          sxx, syy, szz, sxy, syx, sxz, szx, syz, szy (PML stresses), dxux, dyuy, dzuz,
+ *          dxuy, dyux, dxuz, dzux, dyuz, dzuy, then the memory variables Mxx, Myy, Mzz,
+ *          Mxy, Mxz, Myz with the mechanism fastest (fields 18-35 unused when is_diss = 0);
+ *          each field element-major: element i + ex (j + ey k), node in + 5 jn + 25 kn;
+ *   v:     n_events x 3 x G floats -- assembled velocity, component-major, global node
+ *          gx + GX (gy + GY gz), GX = 4 ex + 1, GY = 4 ey + 1.
+ * Zeroed buffers start a run at rest. Model, sources, receivers and the step counter
+ * stay in the handle (set up earlier with the calls above); seismograms are recorded
+ * into the handle. Only plain forward runs (adjoint_flag 0) are accepted.
+ * The element forces between the element and node kernels live in a fixed array in
+ * the library's device memory, 8,388,608 floats (32 MiB), which every GPU that loads
+ * the library holds until the process exits: n_events x 3 x N must not exceed it
+ * (e.g. one event of at most 2,796,202 GLL points); larger runs get SES3D_E_CONFIG.
+ * The first call on a device looks up that array's device address (which may load the
+ * library's device code); make it before any stream capture. Calls that overlap on the
+ * GPU (two handles or threads stepping at once) share the array and race.
+ * The handle's device must be current. No cudaMalloc, cudaFree or other allocating
+ * routine is called. */
+int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int n);
+
 /* Element-kernel block shape: elements per CTA (1, 2 or 4); 0 selects the default.
  * bench.py's autotuner sets it. */
 int ses3d_gpu_set_block_elements(ses3d_gpu *h, int elements_per_cta);

@@ -1030,3 +1030,77 @@ int ses3d_gpu_set_block_elements(ses3d_gpu *h, int elements_per_cta) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free iterations over a caller-owned wavefield (ses3d_gpu_step_external).
+// The element forces, scratch between k_element and k_node, live in this fixed array;
+// its device address is looked up once per device and handed to the kernels.
+// ---------------------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+constexpr size_t kStaticForceFloats = (size_t)8 << 20;  // 8,388,608 floats = 32 MiB
+static __device__ __align__(256) float g_static_forces[kStaticForceFloats];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+float *g_static_forces_ptr[kMaxDevices] = {nullptr};
+
+// Device address of g_static_forces on the current device (looked up on first use).
+int static_forces(ses3d_gpu *h, int dev, float **out) {
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (!g_static_forces_ptr[dev]) {
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_forces);
+    if (e != cudaSuccess || !ptr) return cuda_fail(h, e, "cudaGetSymbolAddress(g_static_forces)");
+    g_static_forces_ptr[dev] = static_cast<float *>(ptr);
+  }
+  *out = g_static_forces_ptr[dev];
+  return SES3D_OK;
+}
+}  // namespace
+
+extern "C" int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int n) {
+  if (!h) return SES3D_E_CONFIG;
+  if (!state || !v) return fail(h, SES3D_E_CONFIG, "null state or velocity buffer");
+  if (n < 0) return fail(h, SES3D_E_CONFIG, "n must be >= 0");
+  if (!h->model_set) return fail(h, SES3D_E_STATE, "set_model must be called before stepping");
+  if (h->mode_flag != 0) return fail(h, SES3D_E_CONFIG, "the external-wavefield step runs plain forward runs only");
+  const size_t need = (size_t)h->cfg.n_events * 3 * (size_t)h->geo.N;
+  if (need > kStaticForceFloats) {
+    char msg[256];
+    std::snprintf(msg, sizeof(msg),
+                  "run needs %zu element-force floats (n_events x 3 x %lld GLL points); the fixed array holds %zu "
+                  "(32 MiB)",
+                  need, (long long)h->geo.N, kStaticForceFloats);
+    return fail(h, SES3D_E_CONFIG, msg);
+  }
+  int dev = -1;
+  CK(h, cudaGetDevice(&dev));
+  if (dev != h->device) return fail(h, SES3D_E_CONFIG, "the handle's device must be current");
+  if (dev < 0 || dev >= kMaxDevices) return fail(h, SES3D_E_CONFIG, "device index out of range");
+  float *forces = nullptr;
+  int rc = static_forces(h, dev, &forces);
+  if (rc) return rc;
+  Ptrs p = make_ptrs(h);
+  p.state = state;
+  p.v = v;
+  p.f = forces;
+  for (int s = 0; s < n && h->it < h->cfg.nt; ++s) {
+    if (h->R > 0) {
+      CK(h, launch_receivers(h->c, v, h->d_rec_elem, h->d_rec_ev, h->d_rec_w, h->d_seis, h->R, h->d_it, h->st));
+      ++h->launches;
+    }
+    CK(h, launch_element(h->cfg.is_diss, 0, h->epb, h->c, p, h->st));
+    ++h->launches;
+    if (h->ngroups) {
+      CK(h, launch_inject(h->c, forces, h->d_groups, h->ngroups, h->d_fdelta, h->d_fstf, h->d_fmask, h->d_it, h->st));
+      ++h->launches;
+    }
+    CK(h, launch_node(h->c, p, h->st));
+    ++h->launches;
+    h->it += 1;
+  }
+  CK(h, cudaStreamSynchronize(h->st));
+  return SES3D_OK;
+}
