@@ -24,7 +24,7 @@ cudaError_t launch_transpose_d(const double *in, double *out, long long rows, lo
 cudaError_t launch_derive(const float *raw, float *mat, float *gm, long long N, int is_diss, float sum_D_p,
                           cudaStream_t st);
 cudaError_t launch_mass(const Consts &c, const float *rhoinv, const float *z, const float *sinx, const float *w,
-                        float Jac, float *MM, cudaStream_t st);
+                        float Jac, float *MM, float *iMM, cudaStream_t st);
 cudaError_t launch_vmax(const float *v, long long G3, int nev, unsigned int *out, cudaStream_t st);
 cudaError_t launch_grad_q_norm(const Consts &c, const float *gm, double *grad, cudaStream_t st);
 cudaError_t launch_gather_ref(const Consts &c, const float *v, float *out, cudaStream_t st);
@@ -137,7 +137,7 @@ Ptrs make_ptrs(ses3d_gpu *h) {
   p.inv_sin = h->d_tab + h->o_isin; p.inv_r = h->d_tab + h->o_ir;
   p.pxr = h->d_tab + h->o_pxr; p.pyr = h->d_tab + h->o_pyr; p.pzr = h->d_tab + h->o_pzr;
   p.pxg = h->d_tab + h->o_pxg; p.pyg = h->d_tab + h->o_pyg; p.pzg = h->d_tab + h->o_pzg;
-  p.MM = h->d_MM; p.mat = h->d_mat; p.gmat = h->d_gmat;
+  p.MM = h->d_MM; p.iMM = h->d_MM + h->geo.G; p.mat = h->d_mat; p.gmat = h->d_gmat;
   p.state = h->d_state; p.v = h->d_v; p.f = h->d_f; p.d_it = h->d_it;
   p.src_elem = h->d_src_elem; p.src_delta = h->d_src_delta; p.src_mom = h->d_src_mom; p.stf = h->d_stf;
   p.grad = h->d_grad;
@@ -268,7 +268,8 @@ int set_model_common(ses3d_gpu *h, float *d_raw) {
     e = launch_transpose(d_tmp + (size_t)(NMAT + f) * N, h->d_gmat + (size_t)f * N, NPE, h->geo.E, h->st);
     if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "transpose gmat"); }
   }
-  e = launch_mass(h->c, d_raw, h->d_tab + h->o_z, h->d_tab + h->o_sin, h->d_tab + h->o_w, h->geo.Jac, h->d_MM, h->st);
+  e = launch_mass(h->c, d_raw, h->d_tab + h->o_z, h->d_tab + h->o_sin, h->d_tab + h->o_w, h->geo.Jac, h->d_MM,
+                  h->d_MM + h->geo.G, h->st);
   if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "mass"); }
   h->launches += 2 + NMAT + NGMAT;
   e = cudaStreamSynchronize(h->st);
@@ -414,7 +415,10 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
                                    cfg->ymax, cfg->zmin, cfg->zmax, cfg->zmax_global);
   if (!msg.empty()) { delete h; return fail(nullptr, SES3D_E_CONFIG, msg); }
   const Geometry &g = h->geo;
-  if (g.N * (long long)cfg->n_events > (1LL << 40)) { delete h; return fail(nullptr, SES3D_E_CONFIG, "mesh too large"); }
+  if (g.N * (long long)cfg->n_events > (1LL << 40) || 3 * g.N >= (1LL << 32) || g.E >= (1LL << 31)) {
+    delete h;
+    return fail(nullptr, SES3D_E_CONFIG, "mesh too large");
+  }
   // constants
   Consts &c = h->c;
   std::memset(&c, 0, sizeof(c));
@@ -466,7 +470,7 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   chk(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
   chk(dalloc(&h->d_ktab, 1));
   chk(dalloc(&h->d_tab, tab.size()));
-  chk(dalloc(&h->d_MM, (size_t)g.G));
+  chk(dalloc(&h->d_MM, (size_t)2 * g.G));  // MM_global and its reciprocal
   chk(dalloc(&h->d_mat, (size_t)NMAT * g.N));
   chk(dalloc(&h->d_gmat, (size_t)NGMAT * g.N));
   chk(dalloc(&h->d_state, nev * NSTATE * g.N));
@@ -491,7 +495,7 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   chk(cudaMemset(h->d_src_delta, 0, nev * NPE * sizeof(float)));
   chk(cudaMemset(h->d_src_mom, 0, nev * 6 * sizeof(float)));
   chk(cudaMemset(h->d_stf, 0, nev * cfg->nt * sizeof(float)));
-  chk(cudaMemset(h->d_MM, 0, (size_t)g.G * sizeof(float)));
+  chk(cudaMemset(h->d_MM, 0, (size_t)2 * g.G * sizeof(float)));
   if (h->d_grad) chk(cudaMemset(h->d_grad, 0, nev * NGRAD * g.N * sizeof(double)));
   if (e != cudaSuccess) {
     std::string m = std::string("initialisation: ") + cudaGetErrorString(e);

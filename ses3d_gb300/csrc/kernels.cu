@@ -303,22 +303,28 @@ __global__ void __launch_bounds__(256) k_node(const Consts c, const Ptrs p) {
   const int gy = (int)(t / (unsigned)c.GX);
   const int gx = (int)t - gy * c.GX;
   const size_t g = (size_t)gz * GXY + t;
+  // node-local loads first: they do not depend on the element forces
+  float *V = p.v + (size_t)ev * 3 * c.G + g;
+  float vx = V[0], vy = V[c.G], vz = V[2 * c.G];
+  const float imm = __ldg(p.iMM + g);
+  const float pxr = __ldg(p.pxg + gx), pyr = __ldg(p.pyg + gy), pzr = __ldg(p.pzg + gz);
   const int i0 = gx == 0 ? 0 : (gx - 1) >> 2, i1 = min(gx >> 2, c.ex - 1);
   const int j0 = gy == 0 ? 0 : (gy - 1) >> 2, j1 = min(gy >> 2, c.ey - 1);
   const int k0 = gz == 0 ? 0 : (gz - 1) >> 2, k1 = min(gz >> 2, c.ez - 1);
-  const size_t N = (size_t)c.N;
-  const float *F = p.f + (size_t)ev * 3 * N;
+  const unsigned N = (unsigned)c.N;  // 3 N < 2^32 is checked at create
+  const float *F = p.f + (size_t)ev * 3 * (size_t)c.N;
   float sx = 0.f, sy = 0.f, sz = 0.f;
-  for (int i = i0; i <= i1; ++i)
+  for (int i = i0; i <= i1; ++i) {
+    const unsigned xi = (unsigned)i * 125u + (unsigned)(gx - 4 * i);
     for (int j = j0; j <= j1; ++j)
       for (int k = k0; k <= k1; ++k) {
-        const size_t q = (size_t)((unsigned)i + (unsigned)c.ex * ((unsigned)j + (unsigned)c.ey * (unsigned)k)) * 125 +
-                         (gx - 4 * i) + 5 * (gy - 4 * j) + 25 * (gz - 4 * k);
+        const unsigned q = xi + (unsigned)c.ex * ((unsigned)j + (unsigned)c.ey * (unsigned)k) * 125u +
+                           (unsigned)(5 * (gy - 4 * j) + 25 * (gz - 4 * k));
         sx += F[q]; sy += F[N + q]; sz += F[2 * N + q];
       }
-  const float mm = p.MM[g];
-  const float ax = sx / mm, ay = sy / mm, az = sz / mm;
-  const float pxr = __ldg(p.pxg + gx), pyr = __ldg(p.pyg + gy), pzr = __ldg(p.pzg + gz);
+  }
+  // a = s / MM with the reciprocal of the mass matrix (ses3d_evolution.f90:318-320)
+  const float ax = sx * imm, ay = sy * imm, az = sz * imm;
   float prof = 0.f, taper = 1.f;
   const float praw = __fadd_rn(__fadd_rn(pxr, pyr), pzr);
   if (praw != 0.f) {
@@ -329,9 +335,7 @@ __global__ void __launch_bounds__(256) k_node(const Consts c, const Ptrs p) {
     prof = __fadd_rn(__fadd_rn(px, py), pz);
     taper = expf(-__fmul_rn(__fmul_rn(0.1f, prof), prof));
   }
-  float *V = p.v + (size_t)ev * 3 * c.G + g;
   const float dt = c.dt;
-  float vx = V[0], vy = V[c.G], vz = V[2 * c.G];
   vx = vx + dt * (ax - prof * vx);
   vy = vy + dt * (ay - prof * vy);
   vz = vz + dt * (az - prof * vz);
@@ -476,7 +480,8 @@ __global__ void k_derive(const float *__restrict__ raw, float *__restrict__ mat,
 // contributions in the reference loop order with IEEE round-to-nearest products, so
 // the result is bit-identical to the reference's FP32 MM_global. rhoinv in reference layout.
 __global__ void k_mass(const Consts c, const float *__restrict__ rhoinv, const float *__restrict__ z,
-                       const float *__restrict__ sinx, const float *__restrict__ w, float Jac, float *__restrict__ MM) {
+                       const float *__restrict__ sinx, const float *__restrict__ w, float Jac, float *__restrict__ MM,
+                       float *__restrict__ iMM) {
   const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= c.G) return;
   const int gx = (int)(g % c.GX);
@@ -502,6 +507,7 @@ __global__ void k_mass(const Consts c, const float *__restrict__ rhoinv, const f
         mm = __fsub_rn(mm, t);
       }
   MM[g] = mm;
+  iMM[g] = __frcp_rn(mm);
 }
 
 // Max |v| per event (NaN-aware watchdog). out: [nev] as float bits, non-negative.
@@ -600,8 +606,8 @@ cudaError_t launch_derive(const float *raw, float *mat, float *gm, long long N, 
 }
 
 cudaError_t launch_mass(const Consts &c, const float *rhoinv, const float *z, const float *sinx, const float *w,
-                        float Jac, float *MM, cudaStream_t st) {
-  k_mass<<<(unsigned)((c.G + 255) / 256), 256, 0, st>>>(c, rhoinv, z, sinx, w, Jac, MM);
+                        float Jac, float *MM, float *iMM, cudaStream_t st) {
+  k_mass<<<(unsigned)((c.G + 255) / 256), 256, 0, st>>>(c, rhoinv, z, sinx, w, Jac, MM, iMM);
   return cudaGetLastError();
 }
 

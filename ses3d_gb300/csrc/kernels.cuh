@@ -53,6 +53,7 @@ struct Ptrs {
   const float *pxr, *pyr, *pzr;         // raw PML per element node
   const float *pxg, *pyg, *pzg;         // raw PML per global index (last writer)
   const float *MM;                      // [G]
+  const float *iMM;                     // [G] 1 / MM
   const float *mat;                     // [NMAT][N]
   const float *gmat;                    // [NGMAT][N] (adjoint)
   float *state;                         // [nev][NSTATE][N]
