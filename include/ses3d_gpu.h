@@ -169,6 +169,19 @@ int ses3d_gpu_record_count(const ses3d_gpu *h, int event);
 int ses3d_gpu_get_record(ses3d_gpu *h, int event, int record, float *out);
 int ses3d_gpu_put_record(ses3d_gpu *h, int event, int record, const float *in);
 
+/* Checkpointed forward-field storage for adjoint runs. With records_per_segment = K > 0
+ * a flag-1 run keeps one full-state checkpoint (element state and assembled velocity of
+ * every event) before every K-th stored iteration instead of the records, and the flag-2
+ * run recomputes the records of one segment at a time from its checkpoint on a second
+ * wavefield (one extra forward pass in total). K = 0 (default) keeps every record in
+ * device memory. Memory with K > 0: ceil(nrec / K) checkpoints of (36 N + 3 G) floats,
+ * K records of 9 N floats and one extra wavefield, per event. Call before the flag-1
+ * run starts. Replaces the disk store/restore of SOURCE/ses3d_output.f90:5-267. */
+int ses3d_gpu_set_checkpointing(ses3d_gpu *h, int records_per_segment);
+
+/* Device memory the handle holds now, in bytes. */
+int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h);
+
 /* saving_vector of the forward run (nt entries; it where stored, else 0);
  * SOURCE/ses3d_main.f90:162 and SOURCE/ses3d_output.f90:379-392. */
 int ses3d_gpu_get_saving_vector(const ses3d_gpu *h, int *out);

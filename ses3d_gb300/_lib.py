@@ -72,6 +72,8 @@ SIGNATURES = {
     "ses3d_gpu_get_saving_vector": (c_int, [c_void_p, P_i]),
     "ses3d_gpu_set_saving_vector": (c_int, [c_void_p, P_i]),
     "ses3d_gpu_begin_adjoint": (c_int, [c_void_p]),
+    "ses3d_gpu_set_checkpointing": (c_int, [c_void_p, c_int]),
+    "ses3d_gpu_memory_bytes": (ctypes.c_int64, [c_void_p]),
     "ses3d_gpu_get_setup_int": (c_long, [c_void_p, c_int, c_char_p, P_i]),
     "ses3d_gpu_get_setup_real": (c_long, [c_void_p, c_int, c_char_p, P_f]),
     "ses3d_gpu_vmax": (c_int, [c_void_p, P_f]),

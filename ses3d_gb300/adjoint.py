@@ -1,0 +1,291 @@
+"""Differentiable waveform misfit: torch.autograd.Function from the model (rho, vp, vsh,
+vsv, Q_mu) to the L2 misfit of band-passed velocity seismograms, whose backward is the
+adjoint solve of the reference (adjoint_flag 2 with time-reversed adjoint sources,
+SOURCE/ses3d_main.f90:142-176) and its Frechet kernels (SOURCE/ses3d_grad.f90:77-83,
+SOURCE/ses3d_grad_Q.f90:115-128).
+
+Model parameters are element-local node values in the reference layout, FP32 tensors on
+the GPU. The model records follow the radially anisotropic mapping of
+MODELS/SOURCE/add_perturbation.f90:512-520 (mu = rho vsh^2, B = rho vsv^2 - mu,
+lambda = rho vp^2 - 2 mu, A = C = 0). The misfit and its time series accumulate in FP64.
+
+Gradient. The kernels K_m of the reference are densities for absolute perturbations of
+(rho at fixed velocities, vp, vsh, vsv) and a relative kernel for Q_mu, integrated with
+the rectangle rule over the stored iterations (weight samp_ad dt) and divided by the
+element Jacobian. The gradient with respect to the value of m at element-local GLL point
+(e, n) is Jac W_(e,n) K_m(e, n), W = w_i w_j w_k Jac r^2 sin(theta) the point's
+quadrature volume; for Q_mu it is divided by Q. This is the continuous-adjoint gradient of
+the reference (not the exact discrete adjoint of the time stepping); the test suite
+reports its agreement with central finite differences.
+
+Adjoint source of a velocity misfit: a(t) = dchi/du_vel(t) = dt F^T F (u - d)(t); the
+force applied in adjoint iteration it is the time derivative of the time-reversed a
+(TOOLS/adjoint_source.py writes the reversed -d/dt of the velocity residual).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+from .solver import Simulation, config_from
+
+
+class Bandpass:
+    """Zero-phase band-pass with a raised-cosine response, applied by zero-padded FFT.
+    Its matrix is symmetric (real even response), so it is its own adjoint."""
+
+    def __init__(self, nt: int, dt: float, fmin: float, fmax: float, taper: float = 0.5):
+        self.nt = nt
+        self.nfft = 1 << int(math.ceil(math.log2(2 * nt)))
+        f = np.fft.rfftfreq(self.nfft, dt)
+        H = np.zeros_like(f)
+        lo0, lo1 = fmin * (1 - taper), fmin
+        hi0, hi1 = fmax, fmax * (1 + taper)
+        H[(f >= lo1) & (f <= hi0)] = 1.0
+        m = (f > lo0) & (f < lo1)
+        H[m] = 0.5 - 0.5 * np.cos(np.pi * (f[m] - lo0) / (lo1 - lo0))
+        m = (f > hi0) & (f < hi1)
+        H[m] = 0.5 + 0.5 * np.cos(np.pi * (f[m] - hi0) / (hi1 - hi0))
+        self.H = H
+
+    def __call__(self, x: np.ndarray) -> np.ndarray:
+        X = np.fft.rfft(np.asarray(x, np.float64), n=self.nfft, axis=-1)
+        return np.fft.irfft(X * self.H, n=self.nfft, axis=-1)[..., : self.nt]
+
+
+def model_records(rho, vp, vsh, vsv, Q):
+    """SES3D model records from (rho, vp, vsh, vsv, Q) tensors (add_perturbation.f90:512-520)."""
+    import torch
+    with torch.no_grad():
+        mu = rho * vsh * vsh
+        rec = {"rhoinv": 1.0 / rho, "mu": mu, "lambda": rho * vp * vp - 2.0 * mu,
+               "A": torch.zeros_like(rho), "B": rho * vsv * vsv - mu, "C": torch.zeros_like(rho), "Q": Q}
+        return {k: v.float().contiguous() for k, v in rec.items()}
+
+
+@dataclass
+class EventData:
+    """One event of an inversion: source, receivers and observed velocity seismograms."""
+    xxs: float
+    yys: float
+    zzs: float
+    source_type: int
+    mom: np.ndarray
+    stf: np.ndarray
+    recloc: np.ndarray               # (nr, 3) colat deg, lon deg, depth m
+    observed: Optional[np.ndarray] = None   # (3, nr, nt) velocity
+
+
+@dataclass
+class MisfitSetup:
+    """Mesh, time axis and events of a misfit; built from a synth.Problem by from_problem."""
+    cfg_template: object
+    events: List[EventData]
+    fmin: float = 1.0 / 50.0
+    fmax: float = 1.0 / 10.0
+    samp_ad: int = 10
+    memory_budget: float = 150e9      # bytes for records/checkpoints of all events
+    grad_q: bool = True
+    last: dict = field(default_factory=dict)
+
+    @classmethod
+    def from_problem(cls, p, n_events: Optional[int] = None, samp_ad: int = 10, **kw) -> "MisfitSetup":
+        nev = len(p.events) if n_events is None else n_events
+        ev0 = p.events[0].event
+        cfg = config_from(p.box, p.setup, ev0.nt, ev0.dt, p.tau, p.D, pml=p.pml, adjoint_flag=1, n_events=nev,
+                          grad_variant=1)
+        cfg.samp_ad = samp_ad
+        evs = [EventData(float(e.event.xxs), float(e.event.yys), float(e.event.zzs), e.event.source_type,
+                         np.asarray(e.event.mom, np.float32), np.asarray(e.stf, np.float32),
+                         np.asarray(e.receivers.loc, np.float32)) for e in p.events[:nev]]
+        return cls(cfg, evs, samp_ad=samp_ad, **kw)
+
+    # -- simulation plumbing --------------------------------------------------------------------
+    def _config(self, adjoint_flag: int):
+        c = L.Config()
+        ctypes_copy(c, self.cfg_template)
+        c.adjoint_flag = adjoint_flag
+        c.samp_ad = self.samp_ad
+        c.n_events = len(self.events)
+        c.grad_variant = 1 if self.grad_q else 0
+        return c
+
+    def simulate(self, records: dict, adjoint: bool = False) -> Simulation:
+        """Forward run of all events on the given model records (device tensors)."""
+        sim = Simulation(self._config(1 if adjoint else 0))
+        sim.set_model_device([records[k].data_ptr() if k in records else 0 for k in
+                              ("rhoinv", "mu", "lambda", "A", "B", "C", "Q")])
+        for k, e in enumerate(self.events):
+            sim.set_source(k, e.xxs, e.yys, e.zzs, e.source_type, e.mom, e.stf)
+            sim.set_receivers(k, e.recloc)
+        if adjoint:
+            K = self.segment_length(sim)
+            if K:
+                L.check(sim.lib.ses3d_gpu_set_checkpointing(sim.h, K), sim.h)
+            self.last["records_per_segment"] = K
+        sim.run()
+        return sim
+
+    def segment_length(self, sim: Simulation) -> int:
+        """0 (keep every record) if all records fit the budget, else the checkpoint segment
+        length K that minimises checkpoint + segment memory."""
+        nt, s = sim.nt, self.samp_ad
+        nrec = len([it for it in range(1, nt + 1) if it % s == 0 or it == 1 or it == nt])
+        rec_b = 9.0 * sim.N * 4 * sim.n_events
+        ck_b = (36.0 * sim.N + 3.0 * sim.G) * 4 * sim.n_events
+        if nrec * rec_b <= self.memory_budget:
+            return 0
+        K = max(1, int(round(math.sqrt(nrec * ck_b / rec_b))))
+        return K
+
+    def filt(self, nt: int, dt: float) -> Bandpass:
+        return Bandpass(nt, dt, self.fmin, self.fmax)
+
+    def seismograms(self, sim: Simulation) -> List[np.ndarray]:
+        out = []
+        for k in range(len(self.events)):
+            sx, sy, sz = sim.seismograms(k)
+            out.append(np.stack([sx, sy, sz]).astype(np.float64))  # (3, nr, nt)
+        return out
+
+    def set_observed(self, model_tensors: Sequence):
+        """Observed data = synthetics of the given (rho, vp, vsh, vsv, Q) model."""
+        sim = self.simulate(model_records(*model_tensors))
+        for e, s in zip(self.events, self.seismograms(sim)):
+            e.observed = s
+        sim.close()
+
+    def misfit_value(self, syn: List[np.ndarray], dt: float) -> float:
+        F = self.filt(syn[0].shape[-1], dt)
+        chi = 0.0
+        for e, s in zip(self.events, syn):
+            r = F(s - e.observed)
+            chi += 0.5 * float(np.sum(r * r)) * dt
+        return chi
+
+    def adjoint_sources(self, syn: List[np.ndarray], dt: float, shift: float = 0.0):
+        """Per event: (nr, 3, nt) forces in adjoint-iteration order. The force density is the
+        functional derivative of chi = 1/2 int |F(u - d)|^2 dt, i.e. F^T F (u - d)(t) per unit
+        time; `shift` delays it by a fraction of a sample (alignment studies)."""
+        nt = syn[0].shape[-1]
+        F = self.filt(nt, dt)
+        out = []
+        for e, s in zip(self.events, syn):
+            a = F(F(s - e.observed))                        # dchi/du_vel(t), (3, nr, nt)
+            if shift:
+                fr = np.fft.rfftfreq(F.nfft, dt)
+                A_ = np.fft.rfft(a, n=F.nfft, axis=-1) * np.exp(-2j * np.pi * fr * shift * dt)
+                a = np.fft.irfft(A_, n=F.nfft, axis=-1)[..., :nt]
+            g = a[..., ::-1]                                # time reversed: adjoint iteration order
+            f = np.gradient(g, dt, axis=-1)                 # d/dtau of the reversed residual
+            out.append(np.ascontiguousarray(np.transpose(f, (1, 0, 2)), np.float32))
+        return out
+
+
+def ctypes_copy(dst, src):
+    for name, _ in src._fields_:
+        v = getattr(src, name)
+        if hasattr(v, "_length_"):
+            arr = getattr(dst, name)
+            for i in range(v._length_):
+                arr[i] = v[i]
+        else:
+            setattr(dst, name, v)
+
+
+def quadrature_volume(sim: Simulation):
+    """W_(e,n) = w_i w_j w_k Jac r^2 sin(theta) in the reference layout (FP64) and Jac."""
+    c = sim.cfg
+    ex, ey, ez = c.nx + 1, c.ny + 1, c.nz + 1
+    w = sim.setup_real("w").astype(np.float64)
+    jac = float(sim.setup_real("Jac")[0])
+    x = sim.setup_real("x").astype(np.float64).reshape(5, ex)   # [in, i]
+    z = sim.setup_real("z").astype(np.float64).reshape(5, ez)   # [kn, k]
+    sin, r2 = np.sin(x), z * z
+    out = np.empty((5, 5, 5, ez, ey, ex))                        # [kn, jn, in, k, j, i]
+    for kn in range(5):
+        for jn in range(5):
+            for in_ in range(5):
+                out[kn, jn, in_] = (w[in_] * w[jn] * w[kn] * jac) * r2[kn][:, None, None] * sin[in_][None, None, :]
+    return out.reshape(-1), jac
+
+
+class _Misfit:
+    """torch.autograd.Function factory (keeps torch an optional import)."""
+
+    @staticmethod
+    def build():
+        import torch
+
+        class WaveformMisfit(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, setup: MisfitSetup, rho, vp, vsh, vsv, Q):
+                recs = model_records(rho, vp, vsh, vsv, Q)
+                sim = setup.simulate(recs, adjoint=True)
+                dt = float(sim.cfg.dt)
+                syn = setup.seismograms(sim)
+                chi = setup.misfit_value(syn, dt)
+                ctx.setup, ctx.sim, ctx.syn, ctx.dt = setup, sim, syn, dt
+                ctx.save_for_backward(Q)
+                setup.last["seismograms"] = syn
+                return torch.tensor(chi, dtype=torch.float64, device=rho.device)
+
+            @staticmethod
+            def backward(ctx, grad_out):
+                (Q,) = ctx.saved_tensors
+                setup, sim, syn, dt = ctx.setup, ctx.sim, ctx.syn, ctx.dt
+                srcs = setup.adjoint_sources(syn, dt, setup.last.get("shift", 0.0))
+                for k, e in enumerate(setup.events):
+                    sim.set_adjoint_sources(k, e.recloc, srcs[k])
+                sim.begin_adjoint()
+                sim.run()
+                W, jac = quadrature_volume(sim)
+                # ses3d's kernel sign convention: dchi = -Jac sum W K dm (checked against FD)
+                scale = -float(grad_out) * jac
+                dev = Q.device
+                grads = []
+                for name in ("rho", "cp", "csh", "csv", "Q_mu"):
+                    g = sum(sim.kernel(name, k) for k in range(sim.n_events)) * W * scale
+                    grads.append(torch.from_numpy(g).to(dev))
+                grads[4] = grads[4] / Q.double()
+                setup.last["kernels"] = {n: g for n, g in zip(("rho", "vp", "vsh", "vsv", "Q"), grads)}
+                sim.close()
+                return (None,) + tuple(g.to(Q.dtype) for g in grads)
+
+        return WaveformMisfit
+
+
+_fn = None
+
+
+def waveform_misfit(setup: MisfitSetup, rho, vp, vsh, vsv, Q):
+    """chi(rho, vp, vsh, vsv, Q) for all events of `setup`; differentiable (backward = adjoint solve)."""
+    global _fn
+    if _fn is None:
+        _fn = _Misfit.build()
+    return _fn.apply(setup, rho, vp, vsh, vsv, Q)
+
+
+def misfit_only(setup: MisfitSetup, rho, vp, vsh, vsv, Q) -> float:
+    """chi without keeping records (finite-difference checks)."""
+    sim = setup.simulate(model_records(rho, vp, vsh, vsv, Q))
+    chi = setup.misfit_value(setup.seismograms(sim), float(sim.cfg.dt))
+    sim.close()
+    return chi
+
+
+def problem_tensors(p, device="cuda"):
+    """(rho, vp, vsh, vsv, Q) tensors of a synth.Problem's model records."""
+    import torch
+    m = p.model
+    rho = 1.0 / m["rhoinv"].astype(np.float64)
+    mu = m["mu"].astype(np.float64)
+    vsh = np.sqrt(mu / rho)
+    vsv = np.sqrt((m["B"].astype(np.float64) + mu) / rho)
+    vp = np.sqrt((m["lambda"].astype(np.float64) + 2 * mu) / rho)
+    Q = m.get("Q", np.full_like(rho, 1e5)).astype(np.float64)
+    return tuple(torch.tensor(a, dtype=torch.float32, device=device) for a in (rho, vp, vsh, vsv, Q))

@@ -44,9 +44,20 @@ struct EventHost {
   std::vector<float> adj_stf;  // [n_local][3][nt]
 };
 
-struct DevBuf {
-  void *p = nullptr;
-  size_t bytes = 0;
+struct ForceSet {
+  int4 *groups = nullptr;
+  float *delta = nullptr, *stf = nullptr;
+  int *mask = nullptr;
+  int n = 0;
+};
+
+// The wavefield an iteration advances: the handle's own, or the recomputing forward run's.
+struct Wave {
+  float *state;
+  float *v;
+  int *d_it;
+  bool adjoint;    // adjoint-run iteration: adjoint forces, no moment source
+  bool receivers;  // record seismograms
 };
 }  // namespace
 
@@ -70,10 +81,8 @@ struct ses3d_gpu {
   int *d_it = nullptr;
   int *d_src_elem = nullptr;
   float *d_src_delta = nullptr, *d_src_mom = nullptr, *d_stf = nullptr;
-  int4 *d_groups = nullptr;
-  float *d_fdelta = nullptr, *d_fstf = nullptr;
-  int *d_fmask = nullptr;
-  int ngroups = 0;
+  int *d_src_none = nullptr;  // all -1: no moment source (adjoint iterations)
+  ForceSet fset[2];           // point forces of the forward (0) and the adjoint (1) runs
   int R = 0;
   int *d_rec_elem = nullptr, *d_rec_ev = nullptr;
   float *d_rec_w = nullptr, *d_seis = nullptr;
@@ -82,6 +91,17 @@ struct ses3d_gpu {
   unsigned int *d_scratch_u = nullptr;
   std::vector<float *> records;  // each [nev][NREC][N]
   int record_cursor = 0;
+  std::vector<int> store_steps;   // iterations whose forward fields are stored (1-based)
+  int nrec_done = 0;              // records produced by the forward run so far
+  // checkpointed storage: a full-state checkpoint before every ckpt_K-th record, records
+  // recomputed segment by segment during the adjoint run
+  int ckpt_K = 0;
+  std::vector<float *> ckpts;     // each [nev][NSTATE N + 3 G]
+  std::vector<int> ckpt_it;       // completed iterations at each checkpoint
+  std::vector<float *> segbuf;    // ckpt_K records of the recomputed segment
+  int seg_loaded = -1;
+  float *d_state2 = nullptr, *d_v2 = nullptr;  // wavefield of the recomputing forward run
+  int *d_it2 = nullptr;
   std::vector<int> saving_vector;  // [nt+1]
   std::vector<EventHost> ev;
   // tables offsets
@@ -151,66 +171,74 @@ void destroy_graph(ses3d_gpu *h) {
   h->graph_dirty = true;
 }
 
-// Rebuild the point-force groups (single forces and adjoint sources) of all events.
+void free_forces(ForceSet &f) {
+  dfree(f.groups); dfree(f.delta); dfree(f.stf); dfree(f.mask);
+  f = ForceSet();
+}
+
+// Rebuild the point-force groups of all events: single forces of the forward run (set 0) and
+// adjoint sources of the adjoint run (set 1). One group per (event, element); a group's
+// sources keep file order.
 int rebuild_forces(ses3d_gpu *h) {
   const int nt = h->cfg.nt;
-  std::map<std::pair<int, long long>, std::vector<int>> groups;  // (event, element) -> sources
-  std::vector<float> delta, stf;
-  std::vector<int> mask;
-  int ns = 0;
-  for (int e = 0; e < h->cfg.n_events; ++e) {
-    const EventHost &E = h->ev[e];
-    const Geometry &g = h->geo;
-    if (h->mode_flag <= 1 && E.src.is_source && E.source_type >= 1 && E.source_type <= 3) {
-      long long el = E.src.isx + (long long)g.ex * (E.src.isy + (long long)g.ey * E.src.isz);
-      groups[{e, el}].push_back(ns++);
-      delta.insert(delta.end(), E.src.delta, E.src.delta + NPE);
-      for (int cc = 0; cc < 3; ++cc) {
-        if (cc == E.source_type - 1) stf.insert(stf.end(), E.so.begin(), E.so.end());
-        else stf.insert(stf.end(), (size_t)nt, 0.f);
-      }
-      mask.push_back(1 << (E.source_type - 1));
-    }
-    if (h->mode_flag == 2) {
-      for (size_t s = 0; s < E.adj.size(); ++s) {
-        const AdjointSource &A = E.adj[s];
-        long long el = A.is[0] + (long long)g.ex * (A.is[1] + (long long)g.ey * A.is[2]);
+  for (int which = 0; which < 2; ++which) {
+    std::map<std::pair<int, long long>, std::vector<int>> groups;  // (event, element) -> sources
+    std::vector<float> delta, stf;
+    std::vector<int> mask;
+    int ns = 0;
+    for (int e = 0; e < h->cfg.n_events; ++e) {
+      const EventHost &E = h->ev[e];
+      const Geometry &g = h->geo;
+      if (which == 0 && E.src.is_source && E.source_type >= 1 && E.source_type <= 3) {
+        long long el = E.src.isx + (long long)g.ex * (E.src.isy + (long long)g.ey * E.src.isz);
         groups[{e, el}].push_back(ns++);
-        delta.insert(delta.end(), A.delta, A.delta + NPE);
-        stf.insert(stf.end(), E.adj_stf.begin() + s * 3 * nt, E.adj_stf.begin() + (s + 1) * 3 * nt);
-        mask.push_back(7);
+        delta.insert(delta.end(), E.src.delta, E.src.delta + NPE);
+        for (int cc = 0; cc < 3; ++cc) {
+          if (cc == E.source_type - 1) stf.insert(stf.end(), E.so.begin(), E.so.end());
+          else stf.insert(stf.end(), (size_t)nt, 0.f);
+        }
+        mask.push_back(1 << (E.source_type - 1));
+      }
+      if (which == 1) {
+        for (size_t s = 0; s < E.adj.size(); ++s) {
+          const AdjointSource &A = E.adj[s];
+          long long el = A.is[0] + (long long)g.ex * (A.is[1] + (long long)g.ey * A.is[2]);
+          groups[{e, el}].push_back(ns++);
+          delta.insert(delta.end(), A.delta, A.delta + NPE);
+          stf.insert(stf.end(), E.adj_stf.begin() + s * 3 * nt, E.adj_stf.begin() + (s + 1) * 3 * nt);
+          mask.push_back(7);
+        }
       }
     }
-  }
-  // flatten: sources of a group contiguous, in file order
-  std::vector<int4> gr;
-  std::vector<float> d2, s2;
-  std::vector<int> m2;
-  int k = 0;
-  for (auto &kv : groups) {
-    int4 g4;
-    g4.x = kv.first.first; g4.y = (int)kv.first.second; g4.z = k;
-    for (int s : kv.second) {
-      d2.insert(d2.end(), delta.begin() + (size_t)s * NPE, delta.begin() + (size_t)(s + 1) * NPE);
-      s2.insert(s2.end(), stf.begin() + (size_t)s * 3 * nt, stf.begin() + (size_t)(s + 1) * 3 * nt);
-      m2.push_back(mask[s]);
-      ++k;
+    std::vector<int4> gr;
+    std::vector<float> d2, s2;
+    std::vector<int> m2;
+    int k = 0;
+    for (auto &kv : groups) {
+      int4 g4;
+      g4.x = kv.first.first; g4.y = (int)kv.first.second; g4.z = k;
+      for (int s : kv.second) {
+        d2.insert(d2.end(), delta.begin() + (size_t)s * NPE, delta.begin() + (size_t)(s + 1) * NPE);
+        s2.insert(s2.end(), stf.begin() + (size_t)s * 3 * nt, stf.begin() + (size_t)(s + 1) * 3 * nt);
+        m2.push_back(mask[s]);
+        ++k;
+      }
+      g4.w = k;
+      gr.push_back(g4);
     }
-    g4.w = k;
-    gr.push_back(g4);
-  }
-  dfree(h->d_groups); dfree(h->d_fdelta); dfree(h->d_fstf); dfree(h->d_fmask);
-  h->d_groups = nullptr; h->d_fdelta = nullptr; h->d_fstf = nullptr; h->d_fmask = nullptr;
-  h->ngroups = (int)gr.size();
-  if (h->ngroups) {
-    CK(h, dalloc(&h->d_groups, gr.size()));
-    CK(h, dalloc(&h->d_fdelta, d2.size()));
-    CK(h, dalloc(&h->d_fstf, s2.size()));
-    CK(h, dalloc(&h->d_fmask, m2.size()));
-    CK(h, cudaMemcpy(h->d_groups, gr.data(), gr.size() * sizeof(int4), cudaMemcpyHostToDevice));
-    CK(h, cudaMemcpy(h->d_fdelta, d2.data(), d2.size() * sizeof(float), cudaMemcpyHostToDevice));
-    CK(h, cudaMemcpy(h->d_fstf, s2.data(), s2.size() * sizeof(float), cudaMemcpyHostToDevice));
-    CK(h, cudaMemcpy(h->d_fmask, m2.data(), m2.size() * sizeof(int), cudaMemcpyHostToDevice));
+    ForceSet &F = h->fset[which];
+    free_forces(F);
+    F.n = (int)gr.size();
+    if (F.n) {
+      CK(h, dalloc(&F.groups, gr.size()));
+      CK(h, dalloc(&F.delta, d2.size()));
+      CK(h, dalloc(&F.stf, s2.size()));
+      CK(h, dalloc(&F.mask, m2.size()));
+      CK(h, cudaMemcpy(F.groups, gr.data(), gr.size() * sizeof(int4), cudaMemcpyHostToDevice));
+      CK(h, cudaMemcpy(F.delta, d2.data(), d2.size() * sizeof(float), cudaMemcpyHostToDevice));
+      CK(h, cudaMemcpy(F.stf, s2.data(), s2.size() * sizeof(float), cudaMemcpyHostToDevice));
+      CK(h, cudaMemcpy(F.mask, m2.data(), m2.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
   }
   destroy_graph(h);
   return SES3D_OK;
@@ -222,7 +250,7 @@ int upload_moment_sources(ses3d_gpu *h) {
   std::vector<float> delta((size_t)nev * NPE, 0.f), stf((size_t)nev * nt, 0.f);
   for (int e = 0; e < nev; ++e) {
     const EventHost &E = h->ev[e];
-    if (h->mode_flag <= 1 && E.src.is_source && E.source_type == 10) {
+    if (E.src.is_source && E.source_type == 10) {
       el[e] = E.src.isx + h->geo.ex * (E.src.isy + h->geo.ey * E.src.isz);
       std::memcpy(&delta[(size_t)e * NPE], E.src.delta, NPE * sizeof(float));
     }
@@ -327,14 +355,22 @@ struct Timed {
   }
 };
 
-// one iteration: receivers, element, inject, node (+ record / kernel work)
-int launch_iteration(ses3d_gpu *h, int mode, float *rec, bool timed = false) {
+Wave primary_wave(ses3d_gpu *h) {
+  return Wave{h->d_state, h->d_v, h->d_it, h->mode_flag == 2, h->mode_flag <= 1};
+}
+
+// one iteration of a wavefield: receivers, element, inject, node (+ record / kernel work)
+int launch_iteration(ses3d_gpu *h, const Wave &w, int mode, float *rec, bool timed = false) {
   Ptrs p = make_ptrs(h);
+  p.state = w.state;
+  p.v = w.v;
+  p.d_it = w.d_it;
   p.rec = rec;
-  const int flag = h->mode_flag;
-  if ((flag == 0 || flag == 1) && h->R > 0) {
+  p.src_elem = w.adjoint ? h->d_src_none : h->d_src_elem;
+  const ForceSet &F = h->fset[w.adjoint ? 1 : 0];
+  if (w.receivers && h->R > 0) {
     Timed t(h, 2, timed);
-    CK(h, launch_receivers(h->c, h->d_v, h->d_rec_elem, h->d_rec_ev, h->d_rec_w, h->d_seis, h->R, h->d_it, h->st));
+    CK(h, launch_receivers(h->c, w.v, h->d_rec_elem, h->d_rec_ev, h->d_rec_w, h->d_seis, h->R, w.d_it, h->st));
     ++h->launches;
   }
   {
@@ -342,9 +378,9 @@ int launch_iteration(ses3d_gpu *h, int mode, float *rec, bool timed = false) {
     CK(h, launch_element(h->cfg.is_diss, mode, h->epb, h->c, p, h->st));
     ++h->launches;
   }
-  if (h->ngroups) {
+  if (F.n) {
     Timed t(h, 3, timed);
-    CK(h, launch_inject(h->c, h->d_f, h->d_groups, h->ngroups, h->d_fdelta, h->d_fstf, h->d_fmask, h->d_it, h->st));
+    CK(h, launch_inject(h->c, h->d_f, F.groups, F.n, F.delta, F.stf, F.mask, w.d_it, h->st));
     ++h->launches;
   }
   {
@@ -355,13 +391,69 @@ int launch_iteration(ses3d_gpu *h, int mode, float *rec, bool timed = false) {
   return SES3D_OK;
 }
 
+// Floats of one full-state checkpoint (all events): element state and assembled velocity.
+size_t ckpt_floats(const ses3d_gpu *h) {
+  return (size_t)h->cfg.n_events * ((size_t)NSTATE * h->geo.N + 3 * (size_t)h->geo.G);
+}
+
+int save_checkpoint(ses3d_gpu *h, int completed_it) {
+  const size_t ns = (size_t)h->cfg.n_events * NSTATE * h->geo.N;
+  float *c = nullptr;
+  CK(h, dalloc(&c, ckpt_floats(h)));
+  h->ckpts.push_back(c);
+  h->ckpt_it.push_back(completed_it);
+  CK(h, cudaMemcpyAsync(c, h->d_state, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  CK(h, cudaMemcpyAsync(c + ns, h->d_v, (size_t)h->cfg.n_events * 3 * h->geo.G * sizeof(float),
+                        cudaMemcpyDeviceToDevice, h->st));
+  return SES3D_OK;
+}
+
+// Recomputes the records of segment s (records s K .. min((s+1) K, nrec) - 1) into segbuf
+// by a forward run from checkpoint s on the second wavefield.
+int recompute_segment(ses3d_gpu *h, int s) {
+  const size_t ns = (size_t)h->cfg.n_events * NSTATE * h->geo.N;
+  const size_t nv = (size_t)h->cfg.n_events * 3 * h->geo.G;
+  const size_t rec_floats = (size_t)h->cfg.n_events * NREC * h->geo.N;
+  if (!h->d_state2) {
+    CK(h, dalloc(&h->d_state2, ns));
+    CK(h, dalloc(&h->d_v2, nv));
+    CK(h, dalloc(&h->d_it2, 1));
+  }
+  while ((int)h->segbuf.size() < h->ckpt_K) {
+    float *r = nullptr;
+    CK(h, dalloc(&r, rec_floats));
+    h->segbuf.push_back(r);
+  }
+  CK(h, cudaMemcpyAsync(h->d_state2, h->ckpts[s], ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  CK(h, cudaMemcpyAsync(h->d_v2, h->ckpts[s] + ns, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  int it0 = h->ckpt_it[s];
+  CK(h, cudaMemcpyAsync(h->d_it2, &h->ckpt_it[s], sizeof(int), cudaMemcpyHostToDevice, h->st));
+  const int r0 = s * h->ckpt_K;
+  const int r1 = std::min((int)h->store_steps.size(), r0 + h->ckpt_K);
+  Wave w{h->d_state2, h->d_v2, h->d_it2, false, false};
+  int r = r0;
+  for (int it = it0 + 1; r < r1; ++it) {
+    float *rec = nullptr;
+    int mode = 0;
+    if (it == h->store_steps[r]) {
+      rec = h->segbuf[r - r0];
+      mode = 1;
+      ++r;
+    }
+    int rc = launch_iteration(h, w, mode, rec);
+    if (rc) return rc;
+  }
+  h->seg_loaded = s;
+  return SES3D_OK;
+}
+
 int build_graph(ses3d_gpu *h) {
   destroy_graph(h);
   cudaGraph_t graph;
   CK(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
   long long before = h->launches;
   for (int s = 0; s < h->graph_n; ++s) {
-    int rc = launch_iteration(h, 0, nullptr);
+    int rc = launch_iteration(h, primary_wave(h), 0, nullptr);
     if (rc) {
       cudaStreamEndCapture(h->st, &graph);
       if (graph) cudaGraphDestroy(graph);
@@ -380,7 +472,7 @@ int build_graph(ses3d_gpu *h) {
 int launches_per_iteration(ses3d_gpu *h) {
   int n = 2;
   if ((h->mode_flag == 0 || h->mode_flag == 1) && h->R > 0) ++n;
-  if (h->ngroups) ++n;
+  if (h->fset[h->mode_flag == 2 ? 1 : 0].n) ++n;
   return n;
 }
 
@@ -478,6 +570,7 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   chk(dalloc(&h->d_f, nev * 3 * g.N));
   chk(dalloc(&h->d_it, 1));
   chk(dalloc(&h->d_src_elem, nev));
+  chk(dalloc(&h->d_src_none, nev));
   chk(dalloc(&h->d_src_delta, nev * NPE));
   chk(dalloc(&h->d_src_mom, nev * 6));
   chk(dalloc(&h->d_stf, nev * cfg->nt));
@@ -492,6 +585,7 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   chk(cudaMemcpy(h->d_tab, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice));
   std::vector<int> minus1(nev, -1);
   chk(cudaMemcpy(h->d_src_elem, minus1.data(), nev * sizeof(int), cudaMemcpyHostToDevice));
+  chk(cudaMemcpy(h->d_src_none, minus1.data(), nev * sizeof(int), cudaMemcpyHostToDevice));
   chk(cudaMemset(h->d_src_delta, 0, nev * NPE * sizeof(float)));
   chk(cudaMemset(h->d_src_mom, 0, nev * 6 * sizeof(float)));
   chk(cudaMemset(h->d_stf, 0, nev * cfg->nt * sizeof(float)));
@@ -505,6 +599,8 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   h->ev.resize(nev);
   h->rec_off.assign(nev + 1, 0);
   h->saving_vector.assign(cfg->nt + 2, 0);
+  for (int it = 1; it <= cfg->nt; ++it)  // stored iterations of a flag-1 run (ses3d_main.f90:144)
+    if (cfg->samp_ad > 0 && (it % cfg->samp_ad == 0 || it == 1 || it == cfg->nt)) h->store_steps.push_back(it);
   int rc = zero_wavefield(h);
   if (rc) { std::string m = h->err; ses3d_gpu_destroy(h); return fail(nullptr, rc, m); }
   cudaStreamSynchronize(h->st);
@@ -519,10 +615,14 @@ int ses3d_gpu_destroy(ses3d_gpu *h) {
   for (auto &pe : h->ev_pending) { h->ev_pool.push_back(pe.second.first); h->ev_pool.push_back(pe.second.second); }
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   void *ptrs[] = {h->d_ktab, h->d_tab, h->d_MM, h->d_mat, h->d_gmat, h->d_state, h->d_v, h->d_f, h->d_it,
-                  h->d_src_elem, h->d_src_delta, h->d_src_mom, h->d_stf, h->d_groups, h->d_fdelta, h->d_fstf,
-                  h->d_fmask, h->d_rec_elem, h->d_rec_ev, h->d_rec_w, h->d_seis, h->d_grad, h->d_scratch_u};
+                  h->d_src_elem, h->d_src_delta, h->d_src_mom, h->d_stf, h->d_src_none, h->d_rec_elem,
+                  h->d_rec_ev, h->d_rec_w, h->d_seis, h->d_grad, h->d_scratch_u, h->d_state2, h->d_v2, h->d_it2};
   for (void *p : ptrs) dfree(p);
+  free_forces(h->fset[0]);
+  free_forces(h->fset[1]);
   for (float *r : h->records) dfree(r);
+  for (float *r : h->ckpts) dfree(r);
+  for (float *r : h->segbuf) dfree(r);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return SES3D_OK;
@@ -664,15 +764,34 @@ int ses3d_gpu_step(ses3d_gpu *h, int n) {
     int mode = 0;
     float *rec = nullptr;
     if (flag == 1 && (it % h->cfg.samp_ad == 0 || it == 1 || it == nt)) {
-      CK(h, dalloc(&rec, (size_t)h->cfg.n_events * NREC * h->geo.N));
-      h->records.push_back(rec);
+      if (h->ckpt_K > 0) {  // checkpoint before every ckpt_K-th record, no records kept
+        if (h->nrec_done % h->ckpt_K == 0) {
+          int rc = save_checkpoint(h, it - 1);
+          if (rc) return rc;
+        }
+      } else {
+        CK(h, dalloc(&rec, (size_t)h->cfg.n_events * NREC * h->geo.N));
+        h->records.push_back(rec);
+        mode = 1;
+      }
+      ++h->nrec_done;
       h->saving_vector[it] = it;
-      mode = 1;
     } else if (flag == 2 && h->saving_vector[nt + 1 - it] > 0 && h->record_cursor > 0) {
-      rec = h->records[--h->record_cursor];
+      const int r = --h->record_cursor;
+      if (h->ckpt_K > 0) {
+        const int s = r / h->ckpt_K;
+        if (s >= (int)h->ckpts.size()) return fail(h, SES3D_E_STATE, "no checkpoint for this record");
+        if (h->seg_loaded != s) {
+          int rc = recompute_segment(h, s);
+          if (rc) return rc;
+        }
+        rec = h->segbuf[r - s * h->ckpt_K];
+      } else {
+        rec = h->records[r];
+      }
       mode = 2;
     }
-    int rc = launch_iteration(h, mode, rec, h->prof_on);
+    int rc = launch_iteration(h, primary_wave(h), mode, rec, h->prof_on);
     if (rc) return rc;
     h->it = it;
     ++done;
@@ -809,12 +928,13 @@ int ses3d_gpu_get_kernel(ses3d_gpu *h, int event, int which, double *out) {
 
 int ses3d_gpu_record_count(const ses3d_gpu *h, int event) {
   if (!h || event < 0 || event >= h->cfg.n_events) return SES3D_E_CONFIG;
-  return (int)h->records.size();
+  return h->ckpt_K > 0 ? h->nrec_done : (int)h->records.size();
 }
 
 int ses3d_gpu_get_record(ses3d_gpu *h, int event, int record, float *out) {
   int rc = check_event(h, event);
   if (rc) return rc;
+  if (h->ckpt_K > 0) return fail(h, SES3D_E_STATE, "records are recomputed from checkpoints, not kept");
   if (record < 0 || record >= (int)h->records.size() || !out) return fail(h, SES3D_E_CONFIG, "bad record index");
   const long long N = h->geo.N;
   float *tmp = nullptr;
@@ -841,6 +961,7 @@ int ses3d_gpu_put_record(ses3d_gpu *h, int event, int record, const float *in) {
     CK(h, cudaMemset(r, 0, (size_t)h->cfg.n_events * NREC * N * sizeof(float)));
     h->records.push_back(r);
     h->record_cursor = (int)h->records.size();
+    h->nrec_done = (int)h->records.size();
   }
   float *tmp = nullptr;
   CK(h, dalloc(&tmp, (size_t)N));
@@ -875,12 +996,10 @@ int ses3d_gpu_begin_adjoint(ses3d_gpu *h) {
     CK(h, dalloc(&h->d_grad, (size_t)h->cfg.n_events * NGRAD * h->geo.N));
   }
   CK(h, cudaMemsetAsync(h->d_grad, 0, (size_t)h->cfg.n_events * NGRAD * h->geo.N * sizeof(double), h->st));
-  h->record_cursor = (int)h->records.size();
+  h->record_cursor = h->ckpt_K > 0 ? h->nrec_done : (int)h->records.size();
+  h->seg_loaded = -1;
+  destroy_graph(h);
   int rc = zero_wavefield(h);
-  if (rc) return rc;
-  rc = upload_moment_sources(h);
-  if (rc) return rc;
-  rc = rebuild_forces(h);
   if (rc) return rc;
   CK(h, cudaStreamSynchronize(h->st));
   return SES3D_OK;
@@ -1008,6 +1127,28 @@ int ses3d_gpu_use_graph(ses3d_gpu *h, int enable, int n_per_graph) {
   return SES3D_OK;
 }
 
+int ses3d_gpu_set_checkpointing(ses3d_gpu *h, int records_per_segment) {
+  if (!h) return SES3D_E_CONFIG;
+  if (records_per_segment < 0) return fail(h, SES3D_E_CONFIG, "records_per_segment must be >= 0");
+  if (h->it != 0 || h->mode_flag != 1) return fail(h, SES3D_E_STATE, "set checkpointing before a flag-1 run starts");
+  h->ckpt_K = records_per_segment;
+  return SES3D_OK;
+}
+
+int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
+  if (!h) return 0;
+  const size_t N = h->geo.N, G = h->geo.G, nev = h->cfg.n_events;
+  size_t f = (size_t)KTAB_FLOATS + 2 * G + (size_t)(NMAT + NGMAT) * N + nev * ((size_t)NSTATE * N + 6 * G);
+  size_t bytes = f * sizeof(float);
+  if (h->d_grad) bytes += nev * NGRAD * N * sizeof(double);
+  bytes += h->records.size() * nev * NREC * N * sizeof(float);
+  bytes += h->ckpts.size() * ckpt_floats(h) * sizeof(float);
+  bytes += h->segbuf.size() * nev * NREC * N * sizeof(float);
+  if (h->d_state2) bytes += nev * ((size_t)NSTATE * N + 3 * G) * sizeof(float);
+  bytes += (size_t)3 * h->cfg.nt * h->R * sizeof(float);
+  return (int64_t)bytes;
+}
+
 int ses3d_gpu_profile(ses3d_gpu *h, int enable) {
   if (!h) return SES3D_E_CONFIG;
   h->prof_on = enable != 0;
@@ -1097,8 +1238,9 @@ extern "C" int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int
     }
     CK(h, launch_element(h->cfg.is_diss, 0, h->epb, h->c, p, h->st));
     ++h->launches;
-    if (h->ngroups) {
-      CK(h, launch_inject(h->c, forces, h->d_groups, h->ngroups, h->d_fdelta, h->d_fstf, h->d_fmask, h->d_it, h->st));
+    if (h->fset[0].n) {
+      const ForceSet &F = h->fset[0];
+      CK(h, launch_inject(h->c, forces, F.groups, F.n, F.delta, F.stf, F.mask, h->d_it, h->st));
       ++h->launches;
     }
     CK(h, launch_node(h->c, p, h->st));

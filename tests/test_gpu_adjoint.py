@@ -73,6 +73,27 @@ def runs(native, oracle_mod, problem):
     return out
 
 
+@pytest.mark.parametrize("K", [1, 3, 100])
+def test_checkpointed_records_give_identical_kernels(native, problem, runs, K):
+    """Checkpoints every K records + segment recompute = keeping every record, bit for bit."""
+    from ses3d_gb300 import _lib
+    from ses3d_gb300.solver import Simulation
+    p = problem
+    sim = Simulation.from_problem(p, adjoint_flag=1, grad_variant=1)
+    _lib.check(sim.lib.ses3d_gpu_set_checkpointing(sim.h, K), sim.h)
+    sim.run()
+    assert sim.record_count() == len(runs["gpu_records"])
+    assert np.array_equal(sim.saving_vector(), runs["gpu_sv"])
+    gseis = sim.seismograms(0)
+    loc, stf = adjoint_inputs(p, gseis)
+    sim.set_adjoint_sources(0, loc, stf)
+    sim.begin_adjoint()
+    sim.run()
+    for k in ("rho", "cp", "csh", "csv", "Q_mu"):
+        assert np.array_equal(sim.kernel(k), runs["gpu_kernels"][k]), k
+    sim.close()
+
+
 def test_saving_vector(runs):
     assert np.array_equal(runs["gpu_sv"], runs["o_sv32"])
     expected = [it if (it % SAMP == 0 or it == 1 or it == NT) else 0 for it in range(1, NT + 1)]

@@ -1,0 +1,84 @@
+"""Differentiable misfit (torch.autograd.Function): the adjoint gradient against central
+finite differences along seeded smooth model directions.
+
+The gradient is the reference's continuous-adjoint kernel gradient (time-reversed adjoint
+solve, rectangle-rule kernel integration), not the exact discrete adjoint; measured
+agreement with FD on this workload is 2-6 % for rho, vp, vsh, vsv. The research Q_mu kernel
+of SOURCE/ses3d_grad_Q.f90 correlates adjoint memory variables with forward strain and
+recovers about half of the FD derivative; the test pins its sign and order of magnitude.
+"""
+import numpy as np
+import pytest
+
+from ses3d_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+ELASTIC_TOL = 0.10
+
+
+@pytest.fixture(scope="module")
+def fd_case(native):
+    import torch
+    from ses3d_gb300 import adjoint as A
+    p = synth.make_problem("small", nt=1500, n_el=(24, 24, 12), seed=41, adjoint_flag=1)
+    setup = A.MisfitSetup.from_problem(p, samp_ad=10, fmin=1 / 80, fmax=1 / 25)
+    m0 = A.problem_tensors(p)
+    truth = synth.build_model(p.box, blob=(0.05, 150e3, 200e3), is_diss=1)
+    setup.set_observed(A.problem_tensors(synth.Problem(p.setup, p.box, p.tau, p.D, truth, p.events, pml=p.pml)))
+    rng = np.random.default_rng(5)
+    ex, ey, ez = p.nx + 1, p.ny + 1, p.nz + 1
+    dirs = [torch.tensor(synth.to_reference_layout(synth.correlated_field(rng, p.box, 150e3).astype(np.float64),
+                                                   ex, ey, ez), device="cuda") for _ in range(5)]
+    scales = [2e-3, 2e-3, 2e-3, 2e-3, 2e-2]
+    deltas = [s * d * m for s, d, m in zip(scales, dirs, m0)]
+    ms = [t.clone().requires_grad_(True) for t in m0]
+    chi = A.waveform_misfit(setup, *ms)
+    chi.backward()
+    out = {}
+    for k, nm in enumerate(("rho", "vp", "vsh", "vsv", "Q")):
+        g = float(torch.sum(ms[k].grad.double() * deltas[k].double()))
+        mp = [t.clone() for t in m0]
+        mm = [t.clone() for t in m0]
+        mp[k] = mp[k] + deltas[k].float()
+        mm[k] = mm[k] - deltas[k].float()
+        fd = (A.misfit_only(setup, *mp) - A.misfit_only(setup, *mm)) / 2
+        out[nm] = (g, fd)
+    return float(chi), out
+
+
+def test_misfit_positive(fd_case):
+    chi, _ = fd_case
+    assert chi > 0 and np.isfinite(chi)
+
+
+@pytest.mark.parametrize("name", ["rho", "vp", "vsh", "vsv"])
+def test_elastic_gradient_matches_finite_differences(fd_case, name):
+    _, out = fd_case
+    g, fd = out[name]
+    assert fd != 0
+    assert abs(g / fd - 1.0) < ELASTIC_TOL, (name, g, fd, g / fd)
+
+
+def test_q_kernel_sign_and_magnitude(fd_case):
+    _, out = fd_case
+    g, fd = out["Q"]
+    assert 0.3 < g / fd < 1.5, (g, fd)
+
+
+def test_checkpointed_gradient_equals_stored(native):
+    """An HBM budget that forces checkpoint + recompute gives the same gradient bit for bit."""
+    import torch
+    from ses3d_gb300 import adjoint as A
+    p = synth.make_problem("tiny", nt=120, seed=43, adjoint_flag=1)
+    grads = []
+    for budget in (1e12, 1.0):
+        setup = A.MisfitSetup.from_problem(p, samp_ad=5, fmin=1 / 40, fmax=1 / 8, memory_budget=budget)
+        setup.set_observed([t * 1.01 for t in A.problem_tensors(p)])
+        ms = [t.clone().requires_grad_(True) for t in A.problem_tensors(p)]
+        chi = A.waveform_misfit(setup, *ms)
+        chi.backward()
+        grads.append([m.grad.cpu().numpy() for m in ms])
+        assert (setup.last["records_per_segment"] > 0) == (budget < 10)
+    for a, b in zip(*grads):
+        assert np.array_equal(a, b)
