@@ -288,9 +288,43 @@ def run_ours(args, rank, world, local):
     }
     if e2e:
         res["e2e"] = e2e
+    if not args.no_batched:
+        res["batched"] = run_batched(args, world)
     if rank == 0 and world == 1 and not args.no_cpu:
         res["cpu_baseline"] = cpu_baseline(p, args.cpu_steps)
     return res
+
+
+def run_batched(args, world):
+    """16 events on one 48x48x24 mesh (uneven receiver counts), one launch sequence per
+    time step for all events, replayed from a CUDA graph; against the same mesh with one event."""
+    import torch
+    from ses3d_gb300 import synth
+    from ses3d_gb300.solver import Simulation
+    steps = args.batched_steps
+    out = {}
+    for nev in (1, 16):
+        p = synth.make_problem("c4", nt=steps + 12, seed=args.seed, n_events=nev)
+        sim = Simulation.from_problem(p)
+        sim.set_block_elements(args.epb or 1)
+        sim.use_graph(True, 10)
+        sim.step(10)
+        stream = torch.cuda.ExternalStream(sim.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sim.step(steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[nev] = (ms, p.n_nodes, [len(e.receivers.names) for e in p.events])
+        sim.close()
+    ms1, n, _ = out[1]
+    ms16, _, nrec = out[16]
+    return {"workload": "c4: 48x48x24 elements, %d GLL points per event, 16 events, receivers per event %d-%d, "
+                        "CUDA graph of 10 iterations" % (n, min(nrec), max(nrec)),
+            "events": 16, "ms_per_step": ms16, "value": world * 16 * n / (ms16 / 1e3), "unit": METRIC,
+            "single_event_ms_per_step": ms1, "per_event_speedup_vs_single": 16 * ms1 / ms16}
 
 
 def run_reference(args, rank, world):
@@ -337,6 +371,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-steps", type=int, default=40)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

@@ -58,3 +58,19 @@ def test_create_rejects_bad_config(native):
     rc = native.ses3d_gpu_create(ctypes.byref(cfg), ctypes.byref(h))
     assert rc == -1
     assert b"lpd" in native.ses3d_gpu_last_error(None)
+
+
+def test_driver_builds_and_reports_missing_gpu(native, tmp_path):
+    """The reference-style driver parses a generated SES3D tree and fails cleanly without a GPU."""
+    import subprocess
+    import torch
+    from ses3d_gb300 import synth
+    drv = os.path.join(ROOT, "ses3d_gb300", "ses3d_gpu_main")
+    assert os.path.exists(drv)
+    assert subprocess.run([drv, "--help"], capture_output=True).returncode == 0
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    p = synth.make_problem("tiny", nt=5, seed=1)
+    synth.write_problem(p, str(tmp_path))
+    res = subprocess.run([drv, "--main", str(tmp_path / "MAIN"), "--pml", "3"], capture_output=True, text=True)
+    assert res.returncode == 1 and "no CUDA device" in res.stderr
