@@ -44,7 +44,7 @@ def fd_case(native):
         mm[k] = mm[k] - deltas[k].float()
         fd = (A.misfit_only(setup, *mp) - A.misfit_only(setup, *mm)) / 2
         out[nm] = (g, fd)
-    return float(chi), out
+    return float(chi.detach()), out
 
 
 def test_misfit_positive(fd_case):
