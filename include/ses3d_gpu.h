@@ -256,6 +256,15 @@ int ses3d_gpu_kernel_time(const ses3d_gpu *h, int which, double *total_ms, int64
  * routine is called. */
 int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int n);
 
+/* Lean plain-forward stepping (adjoint_flag 0 only; off by default). The displacement
+ * gradients dxux..dzuy enter a forward run only through the PML strain terms
+ * (SOURCE/ses3d_evolution.f90:123-134), which vanish outside the PML; with lean stepping
+ * they are read and written only in PML elements, which removes 72 of the 318 bytes the
+ * element kernel moves per GLL point elsewhere. Seismograms, velocities, stresses and
+ * memory variables are unchanged bit for bit; SES3D_FIELD_DXUX..DZUY of non-PML elements
+ * then keep their last values instead of being integrated. */
+int ses3d_gpu_set_lean(ses3d_gpu *h, int enable);
+
 /* Element-kernel block shape: elements per CTA (1, 2 or 4); 0 selects the default.
  * bench.py's autotuner sets it. */
 int ses3d_gpu_set_block_elements(ses3d_gpu *h, int elements_per_cta);

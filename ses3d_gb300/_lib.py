@@ -81,6 +81,7 @@ SIGNATURES = {
     "ses3d_gpu_launch_count": (ctypes.c_int64, [c_void_p]),
     "ses3d_gpu_use_graph": (c_int, [c_void_p, c_int, c_int]),
     "ses3d_gpu_set_block_elements": (c_int, [c_void_p, c_int]),
+    "ses3d_gpu_set_lean": (c_int, [c_void_p, c_int]),
     "ses3d_gpu_step_external": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),
     "ses3d_gpu_profile": (c_int, [c_void_p, c_int]),
     "ses3d_gpu_kernel_time": (c_int, [c_void_p, c_int, P_d, ctypes.POINTER(ctypes.c_int64)]),

@@ -525,6 +525,8 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
     }
   }
   c.s_grad = (float)cfg->samp_ad * cfg->dt;
+  c.pml = cfg->pml;
+  c.lean = 0;
   c.Jac = g.Jac;
   c.inv_jac = 1.f / g.Jac;
   // coefficient tables
@@ -1147,6 +1149,14 @@ int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
   if (h->d_state2) bytes += nev * ((size_t)NSTATE * N + 3 * G) * sizeof(float);
   bytes += (size_t)3 * h->cfg.nt * h->R * sizeof(float);
   return (int64_t)bytes;
+}
+
+int ses3d_gpu_set_lean(ses3d_gpu *h, int enable) {
+  if (!h) return SES3D_E_CONFIG;
+  if (enable && h->mode_flag != 0) return fail(h, SES3D_E_CONFIG, "lean stepping applies to plain forward runs only");
+  h->c.lean = enable ? 1 : 0;
+  destroy_graph(h);
+  return SES3D_OK;
 }
 
 int ses3d_gpu_profile(ses3d_gpu *h, int enable) {

@@ -17,13 +17,17 @@
 #ifndef SES3D_ELEM_MINB
 #define SES3D_ELEM_MINB 6
 #endif
+// The same for k_node (256-thread CTAs).
+#ifndef SES3D_NODE_MINB
+#define SES3D_NODE_MINB 4
+#endif
 
 namespace ses3d {
 
 // ---------------------------------------------------------------------------------------
 // k_element: one element per 128 threads (thread = GLL node), EPB consecutive x-elements
 // per CTA; grid (ceil(ex/EPB), ey, ez * n_events). MODE 0 plain, 1 store forward record,
-// 2 adjoint with kernel correlation. Every independent global load (state, material, v)
+// 2 adjoint with kernel correlation, 3 lean plain (displacement gradients in PML elements only). Every independent global load (state, material, v)
 // is issued before the first barrier so that a thread has all its bytes in flight at once.
 // ---------------------------------------------------------------------------------------
 template <bool DISS, int MODE, int EPB>
@@ -41,7 +45,7 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
   const int j = blockIdx.y;
   const int k = (int)blockIdx.z / c.nev;
   const int ev = (int)blockIdx.z - k * c.nev;
-  const bool act = i < c.ex && n < 125;
+  bool act = i < c.ex && n < 125;
   const int nn = act ? n : 0;
   const int ii = act ? i : 0;
   const int in = nn % 5, jn = (nn / 5) % 5, kn = nn / 25;
@@ -52,16 +56,46 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
   const float *MT = p.mat + m0;
 
   constexpr int NS = DISS ? NSTATE : 18;  // elastic runs carry no memory variables
+  // Outside the PML the displacement gradients enter no output of a plain forward run
+  // (ses3d_evolution.f90:123-134 multiplies them by zero profiles); lean runs skip them there.
+  const bool keep_du =
+      MODE != 3 || i < c.pml || i >= c.ex - c.pml || j < c.pml || j >= c.ey - c.pml || k >= c.ez - c.pml;
   float sv[NS];
   float clam = 0.f, c2mut = 0.f, c2mt = 0.f, cA = 0.f, cB2 = 0.f, cC = 0.f;
   float vx = 0.f, vy = 0.f, vz = 0.f;
+#ifndef SES3D_CHECKED
+  if (MODE == 3)
+#endif
+  {  // index self-check (lean stepping, and every mode in SES3D_CHECKED builds): every index
+     // derived below must lie inside its buffer; a violation is reported and the access skipped
+    const size_t g = (size_t)(ii * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
+    int bad = 0;
+    if (act && (ev < 0 || ev >= c.nev)) bad = 1;
+    if (act && m0 >= N) bad = 2;
+    if (act && g >= (size_t)c.G) bad = 3;
+    if (act && (ii * 5 + in >= c.ex * 5 || j * 5 + jn >= c.ey * 5 || k * 5 + kn >= c.ez * 5)) bad = 4;
+    if (bad) {
+      printf("k_element<%d,%d,%d> bad index kind %d block (%d,%d,%d) thread %d m0 %llu g %llu\n", (int)DISS, MODE, EPB,
+             bad, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, (unsigned long long)m0, (unsigned long long)g);
+      act = false;
+    }
+  }
   if (act) {
     // gather v_global -> element-local v (ses3d_evolution.f90:27-51)
     const size_t g = (size_t)(ii * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
     const float *v = p.v + (size_t)ev * 3 * c.G + g;
     vx = v[0]; vy = v[c.G]; vz = v[2 * c.G];
 #pragma unroll
-    for (int f = 0; f < NS; ++f) sv[f] = S[f * N];
+    for (int f = 0; f < F_DXUX; ++f) sv[f] = S[f * N];
+    if (keep_du) {
+#pragma unroll
+      for (int f = F_DXUX; f <= F_DZUY; ++f) sv[f] = S[f * N];
+    } else {  // lean stepping outside the PML
+#pragma unroll
+      for (int f = F_DXUX; f <= F_DZUY; ++f) sv[f] = 0.f;
+    }
+#pragma unroll
+    for (int f = F_DZUY + 1; f < NS; ++f) sv[f] = S[f * N];
     clam = __ldg(MT + M_CLAM * N); c2mut = __ldg(MT + M_C2MUT * N);
     if (DISS) c2mt = __ldg(MT + M_C2MT * N);
     cA = __ldg(MT + M_A * N); cB2 = __ldg(MT + M_B2 * N); cC = __ldg(MT + M_C * N);
@@ -112,9 +146,11 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
     const float dxuy = sv[F_DXUY] + dt * exy, dyux = sv[F_DYUX] + dt * eyx;
     const float dxuz = sv[F_DXUZ] + dt * exz, dzux = sv[F_DZUX] + dt * ezx;
     const float dyuz = sv[F_DYUZ] + dt * eyz, dzuy = sv[F_DZUY] + dt * ezy;
-    S[F_DXUX * N] = dxux; S[F_DYUY * N] = dyuy; S[F_DZUZ * N] = dzuz;
-    S[F_DXUY * N] = dxuy; S[F_DYUX * N] = dyux; S[F_DXUZ * N] = dxuz;
-    S[F_DZUX * N] = dzux; S[F_DYUZ * N] = dyuz; S[F_DZUY * N] = dzuy;
+    if (keep_du) {
+      S[F_DXUX * N] = dxux; S[F_DYUY * N] = dyuy; S[F_DZUZ * N] = dzuz;
+      S[F_DXUY * N] = dxuy; S[F_DYUX * N] = dyux; S[F_DXUZ * N] = dxuz;
+      S[F_DZUX * N] = dzux; S[F_DYUZ * N] = dyuz; S[F_DZUY * N] = dzuy;
+    }
     // PML profiles of this node (ses3d_init.f90:678-686), corners normalised
     const float pxr = __ldg(p.pxr + ii * 5 + in), pyr = __ldg(p.pyr + j * 5 + jn), pzr = __ldg(p.pzr + k * 5 + kn);
     float px = 0.f, py = 0.f, pz = 0.f, taper = 1.f;
@@ -293,7 +329,7 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
 // ses3d_evolution.f90:286-310), then a = s / MM, v += dt (a - prof v), v *= taper
 // (ses3d_evolution.f90:318-328,366).
 // ---------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_node(const Consts c, const Ptrs p) {
+__global__ void __launch_bounds__(256, SES3D_NODE_MINB) k_node(const Consts c, const Ptrs p) {
   const unsigned t = blockIdx.x * 256u + threadIdx.x;
   const int gz = blockIdx.y, ev = blockIdx.z;
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
@@ -557,13 +593,16 @@ static cudaError_t launch_elem_epb(int epb, const Consts &c, const Ptrs &p, cuda
 }
 
 cudaError_t launch_element(int diss, int mode, int epb, const Consts &c, const Ptrs &p, cudaStream_t st) {
+  if (mode == 0 && c.lean) mode = 3;
   if (diss) {
     if (mode == 1) return launch_elem_epb<true, 1>(epb, c, p, st);
     if (mode == 2) return launch_elem_epb<true, 2>(epb, c, p, st);
+    if (mode == 3) return launch_elem_epb<true, 3>(epb, c, p, st);
     return launch_elem_epb<true, 0>(epb, c, p, st);
   }
   if (mode == 1) return launch_elem_epb<false, 1>(epb, c, p, st);
   if (mode == 2) return launch_elem_epb<false, 2>(epb, c, p, st);
+  if (mode == 3) return launch_elem_epb<false, 3>(epb, c, p, st);
   return launch_elem_epb<false, 0>(epb, c, p, st);
 }
 

@@ -44,6 +44,8 @@ struct Consts {
   float inv_jac;  // unused by the reference-order path; kept for the Q kernels
   float Jac;
   float tau_p[3], D_p[3];
+  int pml;        // PML width in elements
+  int lean;       // plain forward: displacement gradients kept only in PML elements
 };
 
 struct Ptrs {

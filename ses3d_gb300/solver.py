@@ -153,6 +153,10 @@ class Simulation:
     def use_graph(self, enable: bool = True, n_per_graph: int = 10):
         self._check(self.lib.ses3d_gpu_use_graph(self.h, int(enable), int(n_per_graph)))
 
+    def set_lean(self, enable: bool = True):
+        """Plain forward runs: keep displacement gradients only in PML elements (see ses3d_gpu.h)."""
+        self._check(self.lib.ses3d_gpu_set_lean(self.h, int(enable)))
+
     def set_block_elements(self, n: int):
         self._check(self.lib.ses3d_gpu_set_block_elements(self.h, int(n)))
 
