@@ -235,11 +235,12 @@ int ses3d_gpu_kernel_time(const ses3d_gpu *h, int which, double *total_ms, int64
  * in a loop where allocating is not allowed. It has no counterpart in the reference
  * (whose arrays are all static Fortran module variables).
  * The caller owns the wavefield and passes it in device memory:
- *   state: n_events x 36 x N floats -- per event the element-local fields in the order
- *          sxx, syy, szz, sxy, syx, sxz, szx, syz, szy (PML stresses), dxux, dyuy, dzuz,
- *          dxuy, dyux, dxuz, dzux, dyuz, dzuy, then the memory variables Mxx, Myy, Mzz,
- *          Mxy, Mxz, Myz with the mechanism fastest (fields 18-35 unused when is_diss = 0);
- *          each field element-major: element i + ex (j + ey k), node in + 5 jn + 25 kn;
+ *   state: n_events x E x 36 x 125 floats (16-byte aligned) -- per event and element
+ *          (i + ex (j + ey k)) a block of 36 fields of 125 nodes (in + 5 jn + 25 kn), the
+ *          fields in the order sxx, syy, szz, sxy, syx, sxz, szx, syz, szy (PML
+ *          stresses), dxux, dyuy, dzuz, dxuy, dyux, dxuz, dzux, dyuz, dzuy, then the
+ *          memory variables Mxx, Myy, Mzz, Mxy, Mxz, Myz with the mechanism fastest
+ *          (fields 18-35 unused when is_diss = 0);
  *   v:     n_events x 3 x G floats -- assembled velocity, component-major, global node
  *          gx + GX (gy + GY gz), GX = 4 ex + 1, GY = 4 ey + 1.
  * Zeroed buffers start a run at rest. Model, sources, receivers and the step counter

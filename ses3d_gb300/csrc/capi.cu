@@ -28,6 +28,9 @@ cudaError_t launch_mass(const Consts &c, const float *rhoinv, const float *z, co
 cudaError_t launch_vmax(const float *v, long long G3, int nev, unsigned int *out, cudaStream_t st);
 cudaError_t launch_grad_q_norm(const Consts &c, const float *gm, double *grad, cudaStream_t st);
 cudaError_t launch_gather_ref(const Consts &c, const float *v, float *out, cudaStream_t st);
+cudaError_t prepare_element_kernels();
+cudaError_t launch_pack_mat(const float *ref, float *out, long long E, cudaStream_t st);
+cudaError_t launch_state_field(float *state_ev, int field, float *ref, long long E, int to_ref, cudaStream_t st);
 }  // namespace ses3d
 
 using namespace ses3d;
@@ -79,6 +82,7 @@ struct ses3d_gpu {
   float *d_MM = nullptr, *d_mat = nullptr, *d_gmat = nullptr;
   float *d_state = nullptr, *d_v = nullptr, *d_f = nullptr;
   int *d_it = nullptr;
+  int *d_err = nullptr;  // device error word (bounded waits)
   int *d_src_elem = nullptr;
   float *d_src_delta = nullptr, *d_src_mom = nullptr, *d_stf = nullptr;
   int *d_src_none = nullptr;  // all -1: no moment source (adjoint iterations)
@@ -162,6 +166,7 @@ Ptrs make_ptrs(ses3d_gpu *h) {
   p.src_elem = h->d_src_elem; p.src_delta = h->d_src_delta; p.src_mom = h->d_src_mom; p.stf = h->d_stf;
   p.grad = h->d_grad;
   p.grad_q = h->cfg.grad_variant == 1;
+  p.err = h->d_err;
   return p;
 }
 
@@ -288,10 +293,8 @@ int set_model_common(ses3d_gpu *h, float *d_raw) {
   sum_D_p = sum_D_p + h->cfg.D_p[2];
   cudaError_t e = launch_derive(d_raw, d_tmp, d_tmp + (size_t)NMAT * N, N, h->cfg.is_diss, sum_D_p, h->st);
   if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "derive"); }
-  for (int f = 0; f < NMAT; ++f) {
-    e = launch_transpose(d_tmp + (size_t)f * N, h->d_mat + (size_t)f * N, NPE, h->geo.E, h->st);
-    if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "transpose mat"); }
-  }
+  e = launch_pack_mat(d_tmp, h->d_mat, h->geo.E, h->st);
+  if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "pack material"); }
   for (int f = 0; f < NGMAT; ++f) {
     e = launch_transpose(d_tmp + (size_t)(NMAT + f) * N, h->d_gmat + (size_t)f * N, NPE, h->geo.E, h->st);
     if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "transpose gmat"); }
@@ -299,7 +302,7 @@ int set_model_common(ses3d_gpu *h, float *d_raw) {
   e = launch_mass(h->c, d_raw, h->d_tab + h->o_z, h->d_tab + h->o_sin, h->d_tab + h->o_w, h->geo.Jac, h->d_MM,
                   h->d_MM + h->geo.G, h->st);
   if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "mass"); }
-  h->launches += 2 + NMAT + NGMAT;
+  h->launches += 3 + NGMAT;
   e = cudaStreamSynchronize(h->st);
   dfree(d_tmp);
   if (e != cudaSuccess) return cuda_fail(h, e, "set_model");
@@ -565,7 +568,8 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   chk(dalloc(&h->d_ktab, 1));
   chk(dalloc(&h->d_tab, tab.size()));
   chk(dalloc(&h->d_MM, (size_t)2 * g.G));  // MM_global and its reciprocal
-  chk(dalloc(&h->d_mat, (size_t)NMAT * g.N));
+  chk(dalloc(&h->d_mat, (size_t)ELEM_MAT * g.E));
+  chk(dalloc(&h->d_err, 1));
   chk(dalloc(&h->d_gmat, (size_t)NGMAT * g.N));
   chk(dalloc(&h->d_state, nev * NSTATE * g.N));
   chk(dalloc(&h->d_v, nev * 3 * g.G));
@@ -592,6 +596,8 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   chk(cudaMemset(h->d_src_mom, 0, nev * 6 * sizeof(float)));
   chk(cudaMemset(h->d_stf, 0, nev * cfg->nt * sizeof(float)));
   chk(cudaMemset(h->d_MM, 0, (size_t)2 * g.G * sizeof(float)));
+  chk(cudaMemset(h->d_err, 0, sizeof(int)));
+  if (e == cudaSuccess) e = prepare_element_kernels();
   if (h->d_grad) chk(cudaMemset(h->d_grad, 0, nev * NGRAD * g.N * sizeof(double)));
   if (e != cudaSuccess) {
     std::string m = std::string("initialisation: ") + cudaGetErrorString(e);
@@ -618,7 +624,7 @@ int ses3d_gpu_destroy(ses3d_gpu *h) {
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   void *ptrs[] = {h->d_ktab, h->d_tab, h->d_MM, h->d_mat, h->d_gmat, h->d_state, h->d_v, h->d_f, h->d_it,
                   h->d_src_elem, h->d_src_delta, h->d_src_mom, h->d_stf, h->d_src_none, h->d_rec_elem,
-                  h->d_rec_ev, h->d_rec_w, h->d_seis, h->d_grad, h->d_scratch_u, h->d_state2, h->d_v2, h->d_it2};
+                  h->d_rec_ev, h->d_rec_w, h->d_seis, h->d_grad, h->d_scratch_u, h->d_state2, h->d_v2, h->d_it2, h->d_err};
   for (void *p : ptrs) dfree(p);
   free_forces(h->fset[0]);
   free_forces(h->fset[1]);
@@ -743,6 +749,15 @@ int ses3d_gpu_set_adjoint_sources(ses3d_gpu *h, int event, int n, const float *l
   return rebuild_forces(h);
 }
 
+// Reads and clears the device error word after the stream has drained.
+static int check_device_error(ses3d_gpu *h) {
+  int err = 0;
+  CK(h, cudaMemcpy(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err == 0) return SES3D_OK;
+  CK(h, cudaMemset(h->d_err, 0, sizeof(int)));
+  return fail(h, SES3D_E_CUDA, "element kernel: a bulk copy into shared memory did not complete within 2 s");
+}
+
 int ses3d_gpu_step(ses3d_gpu *h, int n) {
   if (!h) return SES3D_E_CONFIG;
   if (!h->model_set) return fail(h, SES3D_E_STATE, "set_model must be called before step");
@@ -804,7 +819,7 @@ int ses3d_gpu_step(ses3d_gpu *h, int n) {
   }
   CK(h, cudaStreamSynchronize(h->st));
   collect_times(h);
-  return SES3D_OK;
+  return check_device_error(h);
 }
 
 int ses3d_gpu_current_step(const ses3d_gpu *h) { return h ? h->it : SES3D_E_CONFIG; }
@@ -862,14 +877,14 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
     e = cudaMemcpyAsync(hout, tmp, N * sizeof(float), cudaMemcpyDeviceToHost, h->st);
     if (e != cudaSuccess) return done(cuda_fail(h, e, "copy"));
   } else if (state_field_index(field) >= 0) {
-    float *d = sbase + (size_t)state_field_index(field) * N;
+    const int f = state_field_index(field);
     cudaError_t e;
     if (hout) {
-      e = launch_transpose(d, tmp, h->geo.E, NPE, h->st);
+      e = launch_state_field(sbase, f, tmp, h->geo.E, 1, h->st);
       if (e == cudaSuccess) e = cudaMemcpyAsync(hout, tmp, N * sizeof(float), cudaMemcpyDeviceToHost, h->st);
     } else {
       e = cudaMemcpyAsync(tmp, hin, N * sizeof(float), cudaMemcpyHostToDevice, h->st);
-      if (e == cudaSuccess) e = launch_transpose(tmp, d, NPE, h->geo.E, h->st);
+      if (e == cudaSuccess) e = launch_state_field(sbase, f, tmp, h->geo.E, 0, h->st);
     }
     if (e != cudaSuccess) return done(cuda_fail(h, e, "field transfer"));
   } else if (field >= SES3D_FIELD_MXX && field <= SES3D_FIELD_MYZ) {
@@ -877,7 +892,7 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
     std::vector<float> buf((size_t)N), inter;
     if (hout) {
       for (int m = 0; m < 3; ++m) {
-        cudaError_t e = launch_transpose(sbase + (size_t)(F_M + 3 * cc + m) * N, tmp, h->geo.E, NPE, h->st);
+        cudaError_t e = launch_state_field(sbase, F_M + 3 * cc + m, tmp, h->geo.E, 1, h->st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(buf.data(), tmp, N * sizeof(float), cudaMemcpyDeviceToHost, h->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
         if (e != cudaSuccess) return done(cuda_fail(h, e, "memory variable transfer"));
@@ -887,7 +902,7 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
       for (int m = 0; m < 3; ++m) {
         for (long long q = 0; q < N; ++q) buf[q] = hin[m + 3 * q];
         cudaError_t e = cudaMemcpyAsync(tmp, buf.data(), N * sizeof(float), cudaMemcpyHostToDevice, h->st);
-        if (e == cudaSuccess) e = launch_transpose(tmp, sbase + (size_t)(F_M + 3 * cc + m) * N, NPE, h->geo.E, h->st);
+        if (e == cudaSuccess) e = launch_state_field(sbase, F_M + 3 * cc + m, tmp, h->geo.E, 0, h->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
         if (e != cudaSuccess) return done(cuda_fail(h, e, "memory variable transfer"));
       }
@@ -1140,7 +1155,8 @@ int ses3d_gpu_set_checkpointing(ses3d_gpu *h, int records_per_segment) {
 int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
   if (!h) return 0;
   const size_t N = h->geo.N, G = h->geo.G, nev = h->cfg.n_events;
-  size_t f = (size_t)KTAB_FLOATS + 2 * G + (size_t)(NMAT + NGMAT) * N + nev * ((size_t)NSTATE * N + 6 * G);
+  size_t f = (size_t)KTAB_FLOATS + 2 * G + (size_t)ELEM_MAT * h->geo.E + (size_t)NGMAT * N +
+             nev * ((size_t)NSTATE * N + 6 * G);
   size_t bytes = f * sizeof(float);
   if (h->d_grad) bytes += nev * NGRAD * N * sizeof(double);
   bytes += h->records.size() * nev * NREC * N * sizeof(float);
@@ -1218,6 +1234,7 @@ int static_forces(ses3d_gpu *h, int dev, float **out) {
 extern "C" int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int n) {
   if (!h) return SES3D_E_CONFIG;
   if (!state || !v) return fail(h, SES3D_E_CONFIG, "null state or velocity buffer");
+  if (reinterpret_cast<uintptr_t>(state) % 16 != 0) return fail(h, SES3D_E_CONFIG, "state buffer must be 16-byte aligned");
   if (n < 0) return fail(h, SES3D_E_CONFIG, "n must be >= 0");
   if (!h->model_set) return fail(h, SES3D_E_STATE, "set_model must be called before stepping");
   if (h->mode_flag != 0) return fail(h, SES3D_E_CONFIG, "the external-wavefield step runs plain forward runs only");
@@ -1258,5 +1275,5 @@ extern "C" int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int
     h->it += 1;
   }
   CK(h, cudaStreamSynchronize(h->st));
-  return SES3D_OK;
+  return check_device_error(h);
 }

@@ -25,87 +25,32 @@
 namespace ses3d {
 
 // ---------------------------------------------------------------------------------------
-// k_element: one element per 128 threads (thread = GLL node), EPB consecutive x-elements
-// per CTA; grid (ceil(ex/EPB), ey, ez * n_events). MODE 0 plain, 1 store forward record,
-// 2 adjoint with kernel correlation, 3 lean plain (displacement gradients in PML elements only). Every independent global load (state, material, v)
-// is issued before the first barrier so that a thread has all its bytes in flight at once.
+// Per-node work of one element after its velocities are in shared memory: strain rates,
+// spherical terms, displacement gradients, PML strain, stress rates, memory variables,
+// PML stress march, moment source, taper, record/kernel epilogues, weak divergence and the
+// element forces. Shared by both element kernels (one barrier inside).
 // ---------------------------------------------------------------------------------------
-template <bool DISS, int MODE, int EPB>
-__global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_ELEM_MINB / EPB : 1)) k_element(const Consts c, const Ptrs p) {
-  __shared__ KTab tab;
-  __shared__ float s_v[EPB][3][TPE];
-  __shared__ float s_p[EPB][9][TPE];
+struct ElemCtx {
+  bool act, keep_du;
+  int n, nn, in, jn, kn, ii, j, k, ev;
+  unsigned e;
+  size_t N, m0;
+  float *S;  // this node's state in global memory: field f at S[f * 125]
+  float vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC;
+};
 
-  for (int t = threadIdx.x; t < KTAB_FLOATS; t += blockDim.x)
-    reinterpret_cast<float *>(&tab)[t] = reinterpret_cast<const float *>(p.ktab)[t];
-
-  const int sub = threadIdx.x / TPE;
-  const int n = threadIdx.x % TPE;
-  const int i = blockIdx.x * EPB + sub;
-  const int j = blockIdx.y;
-  const int k = (int)blockIdx.z / c.nev;
-  const int ev = (int)blockIdx.z - k * c.nev;
-  bool act = i < c.ex && n < 125;
-  const int nn = act ? n : 0;
-  const int ii = act ? i : 0;
-  const int in = nn % 5, jn = (nn / 5) % 5, kn = nn / 25;
-  const unsigned e = (unsigned)ii + (unsigned)c.ex * ((unsigned)j + (unsigned)c.ey * (unsigned)k);
-  const size_t N = (size_t)c.N;
-  const size_t m0 = (size_t)e * 125 + nn;  // material / element-local index
-  float *S = p.state + (size_t)ev * NSTATE * N + m0;
-  const float *MT = p.mat + m0;
-
-  constexpr int NS = DISS ? NSTATE : 18;  // elastic runs carry no memory variables
-  // Outside the PML the displacement gradients enter no output of a plain forward run
-  // (ses3d_evolution.f90:123-134 multiplies them by zero profiles); lean runs skip them there.
-  const bool keep_du =
-      MODE != 3 || i < c.pml || i >= c.ex - c.pml || j < c.pml || j >= c.ey - c.pml || k >= c.ez - c.pml;
-  float sv[NS];
-  float clam = 0.f, c2mut = 0.f, c2mt = 0.f, cA = 0.f, cB2 = 0.f, cC = 0.f;
-  float vx = 0.f, vy = 0.f, vz = 0.f;
-#ifndef SES3D_CHECKED
-  if (MODE == 3)
-#endif
-  {  // index self-check (lean stepping, and every mode in SES3D_CHECKED builds): every index
-     // derived below must lie inside its buffer; a violation is reported and the access skipped
-    const size_t g = (size_t)(ii * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
-    int bad = 0;
-    if (act && (ev < 0 || ev >= c.nev)) bad = 1;
-    if (act && m0 >= N) bad = 2;
-    if (act && g >= (size_t)c.G) bad = 3;
-    if (act && (ii * 5 + in >= c.ex * 5 || j * 5 + jn >= c.ey * 5 || k * 5 + kn >= c.ez * 5)) bad = 4;
-    if (bad) {
-      printf("k_element<%d,%d,%d> bad index kind %d block (%d,%d,%d) thread %d m0 %llu g %llu\n", (int)DISS, MODE, EPB,
-             bad, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, (unsigned long long)m0, (unsigned long long)g);
-      act = false;
-    }
-  }
-  if (act) {
-    // gather v_global -> element-local v (ses3d_evolution.f90:27-51)
-    const size_t g = (size_t)(ii * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
-    const float *v = p.v + (size_t)ev * 3 * c.G + g;
-    vx = v[0]; vy = v[c.G]; vz = v[2 * c.G];
-#pragma unroll
-    for (int f = 0; f < F_DXUX; ++f) sv[f] = S[f * N];
-    if (keep_du) {
-#pragma unroll
-      for (int f = F_DXUX; f <= F_DZUY; ++f) sv[f] = S[f * N];
-    } else {  // lean stepping outside the PML
-#pragma unroll
-      for (int f = F_DXUX; f <= F_DZUY; ++f) sv[f] = 0.f;
-    }
-#pragma unroll
-    for (int f = F_DZUY + 1; f < NS; ++f) sv[f] = S[f * N];
-    clam = __ldg(MT + M_CLAM * N); c2mut = __ldg(MT + M_C2MUT * N);
-    if (DISS) c2mt = __ldg(MT + M_C2MT * N);
-    cA = __ldg(MT + M_A * N); cB2 = __ldg(MT + M_B2 * N); cC = __ldg(MT + M_C * N);
-  } else {
-#pragma unroll
-    for (int f = 0; f < NS; ++f) sv[f] = 0.f;
-  }
-  s_v[sub][0][n] = vx; s_v[sub][1][n] = vy; s_v[sub][2][n] = vz;
-  __syncthreads();
-
+template <bool DISS, int MODE>
+__device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, const KTab &tab, float (*s_v)[TPE],
+                                                float (*s_p)[TPE], const ElemCtx &x, float *sv) {
+  constexpr int NS = DISS ? NSTATE : 18;
+  const bool act = x.act, keep_du = x.keep_du;
+  const int n = x.n, nn = x.nn, in = x.in, jn = x.jn, kn = x.kn, ii = x.ii, j = x.j, k = x.k, ev = x.ev;
+  const unsigned e = x.e;
+  const size_t N = x.N, m0 = x.m0;
+  float *S = x.S;
+  const float vx = x.vx, vy = x.vy, vz = x.vz;
+  const float clam = x.clam, c2mut = x.c2mut, c2mt = x.c2mt, cA = x.cA, cB2 = x.cB2, cC = x.cC;
+  (void)j;
   float r = 1.f, st = 1.f;
   if (act) {
     // strain-rate proxies (ses3d_evolution.f90:57-87)
@@ -114,15 +59,15 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
     for (int q = 0; q < 5; ++q) {
       const int ix = q + 5 * jn + 25 * kn, iy = in + 5 * q + 25 * kn, iz = in + 5 * jn + 25 * q;
       const float dxq = tab.Dx[in][q], dyq = tab.Dy[jn][q], dzq = tab.Dz[kn][q];
-      exx = fmaf(s_v[sub][0][ix], dxq, exx);
-      exy = fmaf(s_v[sub][1][ix], dxq, exy);
-      exz = fmaf(s_v[sub][2][ix], dxq, exz);
-      eyx = fmaf(s_v[sub][0][iy], dyq, eyx);
-      eyy = fmaf(s_v[sub][1][iy], dyq, eyy);
-      eyz = fmaf(s_v[sub][2][iy], dyq, eyz);
-      ezx = fmaf(s_v[sub][0][iz], dzq, ezx);
-      ezy = fmaf(s_v[sub][1][iz], dzq, ezy);
-      ezz = fmaf(s_v[sub][2][iz], dzq, ezz);
+      exx = fmaf(s_v[0][ix], dxq, exx);
+      exy = fmaf(s_v[1][ix], dxq, exy);
+      exz = fmaf(s_v[2][ix], dxq, exz);
+      eyx = fmaf(s_v[0][iy], dyq, eyx);
+      eyy = fmaf(s_v[1][iy], dyq, eyy);
+      eyz = fmaf(s_v[2][iy], dyq, eyz);
+      ezx = fmaf(s_v[0][iz], dzq, ezx);
+      ezy = fmaf(s_v[1][iz], dzq, ezy);
+      ezz = fmaf(s_v[2][iz], dzq, ezz);
     }
     // spherical completion (ses3d_evolution.f90:93-103), divisions by r and r sin(theta)
     // taken as products with the tabulated reciprocals
@@ -147,9 +92,9 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
     const float dxuz = sv[F_DXUZ] + dt * exz, dzux = sv[F_DZUX] + dt * ezx;
     const float dyuz = sv[F_DYUZ] + dt * eyz, dzuy = sv[F_DZUY] + dt * ezy;
     if (keep_du) {
-      S[F_DXUX * N] = dxux; S[F_DYUY * N] = dyuy; S[F_DZUZ * N] = dzuz;
-      S[F_DXUY * N] = dxuy; S[F_DYUX * N] = dyux; S[F_DXUZ * N] = dxuz;
-      S[F_DZUX * N] = dzux; S[F_DYUZ * N] = dyuz; S[F_DZUY * N] = dzuy;
+      S[F_DXUX * 125] = dxux; S[F_DYUY * 125] = dyuy; S[F_DZUZ * 125] = dzuz;
+      S[F_DXUY * 125] = dxuy; S[F_DYUX * 125] = dyux; S[F_DXUZ * 125] = dxuz;
+      S[F_DZUX * 125] = dzux; S[F_DYUZ * 125] = dyuz; S[F_DZUY * 125] = dzuy;
     }
     // PML profiles of this node (ses3d_init.f90:678-686), corners normalised
     const float pxr = __ldg(p.pxr + ii * 5 + in), pyr = __ldg(p.pyr + j * 5 + jn), pzr = __ldg(p.pzr + k * 5 + kn);
@@ -201,7 +146,7 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
           float M = Mv[3 * cc + m];
           M = M - M * c.a_k[m] - c.L_k[m] * ecomp[cc];
           Mv[3 * cc + m] = M;
-          S[(F_M + 3 * cc + m) * N] = M;
+          S[(F_M + 3 * cc + m) * 125] = M;
         }
     } else {
       const float Lw = clam * tr;
@@ -226,9 +171,9 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
     s_yz = s_yz + dt * (syz - py * s_yz);
     s_zy = s_zy + dt * (syz - pz * s_zy);
     // taper (ses3d_evolution.f90:368-371); the divergence below uses the untapered values
-    S[F_SXX * N] = s_xx * taper; S[F_SYY * N] = s_yy * taper; S[F_SZZ * N] = s_zz * taper;
-    S[F_SXY * N] = s_xy * taper; S[F_SYX * N] = s_yx * taper; S[F_SXZ * N] = s_xz * taper;
-    S[F_SZX * N] = s_zx * taper; S[F_SYZ * N] = s_yz * taper; S[F_SZY * N] = s_zy * taper;
+    S[F_SXX * 125] = s_xx * taper; S[F_SYY * 125] = s_yy * taper; S[F_SZZ * 125] = s_zz * taper;
+    S[F_SXY * 125] = s_xy * taper; S[F_SYX * 125] = s_yx * taper; S[F_SXZ * 125] = s_xz * taper;
+    S[F_SZX * 125] = s_zx * taper; S[F_SYZ * 125] = s_yz * taper; S[F_SZY * 125] = s_zy * taper;
     // moment-tensor source field (ses3d_miscellaneous.f90:115-147)
     if (MODE != 2 && (int)e == __ldg(p.src_elem + ev)) {
       const int it = *p.d_it + 1;
@@ -243,9 +188,9 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
     }
     // node-local weights of the weak divergence (ses3d_evolution.f90:247-249)
     const float wx = tab.w[in] * st, wy = tab.w[jn], wz = tab.w[kn] * r * r;
-    s_p[sub][0][n] = wx * s_xx; s_p[sub][1][n] = wx * s_xy; s_p[sub][2][n] = wx * s_xz;
-    s_p[sub][3][n] = wy * s_yx; s_p[sub][4][n] = wy * s_yy; s_p[sub][5][n] = wy * s_yz;
-    s_p[sub][6][n] = wz * s_zx; s_p[sub][7][n] = wz * s_zy; s_p[sub][8][n] = wz * s_zz;
+    s_p[0][n] = wx * s_xx; s_p[1][n] = wx * s_xy; s_p[2][n] = wx * s_xz;
+    s_p[3][n] = wy * s_yx; s_p[4][n] = wy * s_yy; s_p[5][n] = wy * s_yz;
+    s_p[6][n] = wz * s_zx; s_p[7][n] = wz * s_zy; s_p[8][n] = wz * s_zz;
 
     if (MODE == 1) {  // forward record (ses3d_main.f90:148-158)
       float *R = p.rec + (size_t)ev * NREC * N + m0;
@@ -305,21 +250,300 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
     for (int q = 0; q < 5; ++q) {
       const int ix = q + 5 * jn + 25 * kn, iy = in + 5 * q + 25 * kn, iz = in + 5 * jn + 25 * q;
       const float dxq = tab.dlT[in][q], dyq = tab.dlT[jn][q], dzq = tab.dlT[kn][q];
-      ax0 = fmaf(s_p[sub][0][ix], dxq, ax0);
-      ax1 = fmaf(s_p[sub][1][ix], dxq, ax1);
-      ax2 = fmaf(s_p[sub][2][ix], dxq, ax2);
-      ay0 = fmaf(s_p[sub][3][iy], dyq, ay0);
-      ay1 = fmaf(s_p[sub][4][iy], dyq, ay1);
-      ay2 = fmaf(s_p[sub][5][iy], dyq, ay2);
-      az0 = fmaf(s_p[sub][6][iz], dzq, az0);
-      az1 = fmaf(s_p[sub][7][iz], dzq, az1);
-      az2 = fmaf(s_p[sub][8][iz], dzq, az2);
+      ax0 = fmaf(s_p[0][ix], dxq, ax0);
+      ax1 = fmaf(s_p[1][ix], dxq, ax1);
+      ax2 = fmaf(s_p[2][ix], dxq, ax2);
+      ay0 = fmaf(s_p[3][iy], dyq, ay0);
+      ay1 = fmaf(s_p[4][iy], dyq, ay1);
+      ay2 = fmaf(s_p[5][iy], dyq, ay2);
+      az0 = fmaf(s_p[6][iz], dzq, az0);
+      az1 = fmaf(s_p[7][iz], dzq, az1);
+      az2 = fmaf(s_p[8][iz], dzq, az2);
     }
     const float cx = tab.CX[jn][kn] * r, cy = tab.CY[in][kn] * r, cz = tab.CZ[in][jn] * st;
-    float *F = p.f + (size_t)ev * 3 * N + m0;
+    float *F = p.f + ((size_t)ev * c.E + e) * 375 + nn;
     F[0] = cx * ax0 + cy * ay0 + cz * az0;
-    F[N] = cx * ax1 + cy * ay1 + cz * az1;
-    F[2 * N] = cx * ax2 + cy * ay2 + cz * az2;
+    F[125] = cx * ax1 + cy * ay1 + cz * az1;
+    F[250] = cx * ax2 + cy * ay2 + cz * az2;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// k_element: one element per 128 threads (thread = GLL node), EPB consecutive x-elements
+// per CTA; grid (ceil(ex/EPB), ey, ez * n_events). MODE 0 plain, 1 store forward record,
+// 2 adjoint with kernel correlation, 3 lean plain (displacement gradients in PML elements only). Every independent global load (state, material, v)
+// is issued before the first barrier so that a thread has all its bytes in flight at once.
+// ---------------------------------------------------------------------------------------
+template <bool DISS, int MODE, int EPB>
+__global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_ELEM_MINB / EPB : 1)) k_element(const Consts c, const Ptrs p) {
+  __shared__ KTab tab;
+  __shared__ float s_v[EPB][3][TPE];
+  __shared__ float s_p[EPB][9][TPE];
+
+  for (int t = threadIdx.x; t < KTAB_FLOATS; t += blockDim.x)
+    reinterpret_cast<float *>(&tab)[t] = reinterpret_cast<const float *>(p.ktab)[t];
+
+  const int sub = threadIdx.x / TPE;
+  const int n = threadIdx.x % TPE;
+  const int i = blockIdx.x * EPB + sub;
+  const int j = blockIdx.y;
+  const int k = (int)blockIdx.z / c.nev;
+  const int ev = (int)blockIdx.z - k * c.nev;
+  bool act = i < c.ex && n < 125;
+  const int nn = act ? n : 0;
+  const int ii = act ? i : 0;
+  const int in = nn % 5, jn = (nn / 5) % 5, kn = nn / 25;
+  const unsigned e = (unsigned)ii + (unsigned)c.ex * ((unsigned)j + (unsigned)c.ey * (unsigned)k);
+  const size_t N = (size_t)c.N;
+  const size_t m0 = (size_t)e * 125 + nn;  // element-major index of field-major arrays (records, gmat)
+  float *S = p.state + ((size_t)ev * c.E + e) * ELEM_STATE + nn;  // field f at S[f * 125]
+  const float *MT = p.mat + (size_t)e * ELEM_MAT + nn;             // field f at MT[f * MAT_ROW]
+
+  constexpr int NS = DISS ? NSTATE : 18;  // elastic runs carry no memory variables
+  // Outside the PML the displacement gradients enter no output of a plain forward run
+  // (ses3d_evolution.f90:123-134 multiplies them by zero profiles); lean runs skip them there.
+  const bool keep_du =
+      MODE != 3 || i < c.pml || i >= c.ex - c.pml || j < c.pml || j >= c.ey - c.pml || k >= c.ez - c.pml;
+  float sv[NS];
+  float clam = 0.f, c2mut = 0.f, c2mt = 0.f, cA = 0.f, cB2 = 0.f, cC = 0.f;
+  float vx = 0.f, vy = 0.f, vz = 0.f;
+#ifndef SES3D_CHECKED
+  if (MODE == 3)
+#endif
+  {  // index self-check (lean stepping, and every mode in SES3D_CHECKED builds): every index
+     // derived below must lie inside its buffer; a violation is reported and the access skipped
+    const size_t g = (size_t)(ii * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
+    int bad = 0;
+    if (act && (ev < 0 || ev >= c.nev)) bad = 1;
+    if (act && m0 >= N) bad = 2;
+    if (act && g >= (size_t)c.G) bad = 3;
+    if (act && (ii * 5 + in >= c.ex * 5 || j * 5 + jn >= c.ey * 5 || k * 5 + kn >= c.ez * 5)) bad = 4;
+    if (bad) {
+      printf("k_element<%d,%d,%d> bad index kind %d block (%d,%d,%d) thread %d m0 %llu g %llu\n", (int)DISS, MODE, EPB,
+             bad, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, (unsigned long long)m0, (unsigned long long)g);
+      act = false;
+    }
+  }
+  if (act) {
+    // gather v_global -> element-local v (ses3d_evolution.f90:27-51)
+    const size_t g = (size_t)(ii * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
+    const float *v = p.v + (size_t)ev * 3 * c.G + g;
+    vx = v[0]; vy = v[c.G]; vz = v[2 * c.G];
+#pragma unroll
+    for (int f = 0; f < F_DXUX; ++f) sv[f] = S[f * 125];
+    if (keep_du) {
+#pragma unroll
+      for (int f = F_DXUX; f <= F_DZUY; ++f) sv[f] = S[f * 125];
+    } else {  // lean stepping outside the PML
+#pragma unroll
+      for (int f = F_DXUX; f <= F_DZUY; ++f) sv[f] = 0.f;
+    }
+#pragma unroll
+    for (int f = F_DZUY + 1; f < NS; ++f) sv[f] = S[f * 125];
+    clam = __ldg(MT + M_CLAM * MAT_ROW); c2mut = __ldg(MT + M_C2MUT * MAT_ROW);
+    if (DISS) c2mt = __ldg(MT + M_C2MT * MAT_ROW);
+    cA = __ldg(MT + M_A * MAT_ROW); cB2 = __ldg(MT + M_B2 * MAT_ROW); cC = __ldg(MT + M_C * MAT_ROW);
+  } else {
+#pragma unroll
+    for (int f = 0; f < NS; ++f) sv[f] = 0.f;
+  }
+  s_v[sub][0][n] = vx; s_v[sub][1][n] = vy; s_v[sub][2][n] = vz;
+  __syncthreads();
+  ElemCtx x{act, keep_du, n, nn, in, jn, kn, ii, j, k, ev, e, N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC};
+  element_compute<DISS, MODE>(c, p, tab, s_v[sub], s_p[sub], x, sv);
+}
+
+
+// ---------------------------------------------------------------------------------------
+// k_element_tma: persistent element kernel for plain and lean forward iterations. Each
+// 128-thread CTA walks (element, event) items with a stride of the grid; one thread copies
+// an item's whole state block (18,000 B) and material block (3,072 B) into shared memory
+// with cp.async.bulk on an mbarrier, two items ahead of the compute, so the loads leave the
+// register file and overlap the previous item's arithmetic. Results equal k_element's bit
+// for bit (same arithmetic, only the source of the loaded values differs).
+// Every mbarrier wait is bounded (2 s of %globaltimer): on expiry the block records an
+// error in p.err, waits (bounded again) for its copies still in flight and returns; the
+// host reports the failed step.
+// ---------------------------------------------------------------------------------------
+constexpr int TMA_STAGES = 2;
+struct __align__(16) ElemStage {
+  float state[ELEM_STATE];  // 18,000 B
+  float mat[ELEM_MAT];      // 3,072 B
+};
+constexpr size_t TMA_BAR_OFF = TMA_STAGES * sizeof(ElemStage) + 12 * TPE * sizeof(float) + ((sizeof(KTab) + 15) / 16) * 16;
+constexpr size_t TMA_SMEM = TMA_BAR_OFF + TMA_STAGES * sizeof(unsigned long long);
+
+__device__ __forceinline__ unsigned smem_addr(const void *ptr) { return (unsigned)__cvta_generic_to_shared(ptr); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.u32 %0, 1, 0, P;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits for phase `parity` of bar; gives up after 2 s, recording the failure in *err.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity, int *err) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (global_ns() - t0 > 2000000000ull) {
+      atomicExch(err, 2);
+      return false;
+    }
+  }
+  return true;
+}
+
+// 1-D bulk copy global -> shared, completing on bar (addresses 16-B aligned, bytes % 16 == 0).
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ bool in_pml_element(const Consts &c, int i, int j, int k) {
+  return i < c.pml || i >= c.ex - c.pml || j < c.pml || j >= c.ey - c.pml || k >= c.ez - c.pml;
+}
+
+// Copies of one item into a stage. Byte ranges (element block of 18,000 B, fields of 500 B):
+// all 36 fields; elastic: fields 0-17 (9,008 B, the last 8 B inside field 18); lean outside
+// the PML: fields 0-8 (4,512 B) and, with attenuation, 18-35 (from byte 8,992, 9,008 B),
+// skipping the displacement gradients. Every range starts and ends 16-B aligned inside the block.
+template <bool DISS, int MODE>
+__device__ __forceinline__ void issue_item(const Consts &c, const Ptrs &p, long long item, ElemStage *st,
+                                           unsigned long long *bar) {
+  const int ev = (int)(item % c.nev);
+  const unsigned e = (unsigned)(item / c.nev);
+  const int i = (int)(e % (unsigned)c.ex), j = (int)((e / (unsigned)c.ex) % (unsigned)c.ey);
+  const int k = (int)(e / ((unsigned)c.ex * (unsigned)c.ey));
+  const char *src = reinterpret_cast<const char *>(p.state + ((size_t)ev * c.E + e) * ELEM_STATE);
+  const char *msrc = reinterpret_cast<const char *>(p.mat + (size_t)e * ELEM_MAT);
+  char *dst = reinterpret_cast<char *>(st->state);
+  constexpr unsigned MB = ELEM_MAT * sizeof(float);
+  if (!DISS && MODE == 3 && !in_pml_element(c, i, j, k)) {
+    mbar_arrive_expect_tx(bar, 4512u + MB);
+    bulk_g2s(dst, src, 4512u, bar);
+  } else if (!DISS) {
+    mbar_arrive_expect_tx(bar, 9008u + MB);
+    bulk_g2s(dst, src, 9008u, bar);
+  } else if (MODE == 3 && !in_pml_element(c, i, j, k)) {
+    mbar_arrive_expect_tx(bar, 4512u + 9008u + MB);
+    bulk_g2s(dst, src, 4512u, bar);
+    bulk_g2s(dst + 8992, src + 8992, 9008u, bar);
+  } else {
+    mbar_arrive_expect_tx(bar, (unsigned)(ELEM_STATE * sizeof(float)) + MB);
+    bulk_g2s(dst, src, (unsigned)(ELEM_STATE * sizeof(float)), bar);
+  }
+  bulk_g2s(st->mat, msrc, MB, bar);
+}
+
+template <bool DISS, int MODE>
+__global__ void __launch_bounds__(TPE, 4) k_element_tma(const Consts c, const Ptrs p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  ElemStage *stage = reinterpret_cast<ElemStage *>(smem);
+  float (*s_v)[TPE] = reinterpret_cast<float (*)[TPE]>(smem + TMA_STAGES * sizeof(ElemStage));
+  float (*s_p)[TPE] = s_v + 3;
+  KTab *tab = reinterpret_cast<KTab *>(s_p + 9);
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + TMA_BAR_OFF);
+
+  const int n = threadIdx.x;
+  const long long total = c.E * (long long)c.nev;
+  const long long first = blockIdx.x, stride = gridDim.x;
+  if (n == 0) {
+    for (int s = 0; s < TMA_STAGES; ++s) mbar_init(&bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int t = n; t < KTAB_FLOATS; t += TPE)
+    reinterpret_cast<float *>(tab)[t] = reinterpret_cast<const float *>(p.ktab)[t];
+  __syncthreads();
+  if (n == 0)
+    for (int s = 0; s < TMA_STAGES; ++s)
+      if (first + s * stride < total) issue_item<DISS, MODE>(c, p, first + s * stride, &stage[s], &bar[s]);
+
+  constexpr int NS = DISS ? NSTATE : 18;
+  const bool on = n < 125;
+  const int nn = on ? n : 0;
+  const int in = nn % 5, jn = (nn / 5) % 5, kn = nn / 25;
+  for (int t = 0;; ++t) {
+    const long long item = first + (long long)t * stride;
+    if (item >= total) break;
+    const int s = t % TMA_STAGES;
+    const unsigned parity = (unsigned)(t / TMA_STAGES) & 1u;
+    const int ev = (int)(item % c.nev);
+    const unsigned e = (unsigned)(item / c.nev);
+    const int i = (int)(e % (unsigned)c.ex), j = (int)((e / (unsigned)c.ex) % (unsigned)c.ey);
+    const int k = (int)(e / ((unsigned)c.ex * (unsigned)c.ey));
+    const bool keep_du = MODE != 3 || in_pml_element(c, i, j, k);
+    // gather v_global -> element-local v (ses3d_evolution.f90:27-51), issued before the wait
+    float vx = 0.f, vy = 0.f, vz = 0.f;
+    if (on) {
+      const size_t g = (size_t)(i * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
+      const float *v = p.v + (size_t)ev * 3 * c.G + g;
+      vx = v[0]; vy = v[c.G]; vz = v[2 * c.G];
+    }
+    const bool ok = mbar_wait_bounded(&bar[s], parity, p.err);
+    float sv[NS];
+    float clam = 0.f, c2mut = 0.f, c2mt = 0.f, cA = 0.f, cB2 = 0.f, cC = 0.f;
+    if (on) {
+      const float *ss = stage[s].state + nn;
+      const float *sm = stage[s].mat + nn;
+#pragma unroll
+      for (int f = 0; f < F_DXUX; ++f) sv[f] = ss[f * 125];
+      if (keep_du) {
+#pragma unroll
+        for (int f = F_DXUX; f <= F_DZUY; ++f) sv[f] = ss[f * 125];
+      } else {
+#pragma unroll
+        for (int f = F_DXUX; f <= F_DZUY; ++f) sv[f] = 0.f;
+      }
+#pragma unroll
+      for (int f = F_DZUY + 1; f < NS; ++f) sv[f] = ss[f * 125];
+      clam = sm[M_CLAM * MAT_ROW]; c2mut = sm[M_C2MUT * MAT_ROW];
+      if (DISS) c2mt = sm[M_C2MT * MAT_ROW];
+      cA = sm[M_A * MAT_ROW]; cB2 = sm[M_B2 * MAT_ROW]; cC = sm[M_C * MAT_ROW];
+    } else {
+#pragma unroll
+      for (int f = 0; f < NS; ++f) sv[f] = 0.f;
+    }
+    s_v[0][n] = vx; s_v[1][n] = vy; s_v[2][n] = vz;
+    if (__syncthreads_or(!ok)) {  // a copy never arrived: drain both stages, then leave
+      if (n == 0) {
+        mbar_wait_bounded(&bar[s], parity, p.err);
+        if (item + stride < total) mbar_wait_bounded(&bar[s ^ 1], (unsigned)((t + 1) / TMA_STAGES) & 1u, p.err);
+      }
+      return;
+    }
+    // stage s fully read, s_v complete
+    if (n == 0) {
+      const long long next = item + TMA_STAGES * stride;
+      if (next < total) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue_item<DISS, MODE>(c, p, next, &stage[s], &bar[s]);
+      }
+    }
+    const size_t m0 = (size_t)e * 125 + nn;
+    float *S = p.state + ((size_t)ev * c.E + e) * ELEM_STATE + nn;
+    ElemCtx x{on, keep_du, n, nn, in, jn, kn, i, j, k, ev, e, (size_t)c.N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC};
+    element_compute<DISS, (MODE == 3 ? 3 : 0)>(c, p, *tab, s_v, s_p, x, sv);
   }
 }
 
@@ -347,16 +571,15 @@ __global__ void __launch_bounds__(256, SES3D_NODE_MINB) k_node(const Consts c, c
   const int i0 = gx == 0 ? 0 : (gx - 1) >> 2, i1 = min(gx >> 2, c.ex - 1);
   const int j0 = gy == 0 ? 0 : (gy - 1) >> 2, j1 = min(gy >> 2, c.ey - 1);
   const int k0 = gz == 0 ? 0 : (gz - 1) >> 2, k1 = min(gz >> 2, c.ez - 1);
-  const unsigned N = (unsigned)c.N;  // 3 N < 2^32 is checked at create
-  const float *F = p.f + (size_t)ev * 3 * (size_t)c.N;
+  const float *F = p.f + (size_t)ev * 3 * (size_t)c.N;  // [E][3][125]; 3 N < 2^32 is checked at create
   float sx = 0.f, sy = 0.f, sz = 0.f;
   for (int i = i0; i <= i1; ++i) {
-    const unsigned xi = (unsigned)i * 125u + (unsigned)(gx - 4 * i);
+    const unsigned xi = (unsigned)i * 375u + (unsigned)(gx - 4 * i);
     for (int j = j0; j <= j1; ++j)
       for (int k = k0; k <= k1; ++k) {
-        const unsigned q = xi + (unsigned)c.ex * ((unsigned)j + (unsigned)c.ey * (unsigned)k) * 125u +
+        const unsigned q = xi + (unsigned)c.ex * ((unsigned)j + (unsigned)c.ey * (unsigned)k) * 375u +
                            (unsigned)(5 * (gy - 4 * j) + 25 * (gz - 4 * k));
-        sx += F[q]; sy += F[N + q]; sz += F[2 * N + q];
+        sx += F[q]; sy += F[q + 125]; sz += F[q + 250];
       }
   }
   // a = s / MM with the reciprocal of the mass matrix (ses3d_evolution.f90:318-320)
@@ -428,8 +651,8 @@ __global__ void __launch_bounds__(128) k_inject(const Consts c, float *__restric
   if (n >= 125) return;
   const int it = *d_it + 1;
   const long long N = c.N;
-  float *F = f + (long long)gr.x * 3 * N + (long long)gr.y * 125 + n;
-  float fx = F[0], fy = F[N], fz = F[2 * N];
+  float *F = f + ((long long)gr.x * c.E + gr.y) * 375 + n;  // [event][element][3][125]
+  float fx = F[0], fy = F[125], fz = F[250];
   for (int s = gr.z; s < gr.w; ++s) {
     const float d = delta[(long long)s * 125 + n];
     const float *S = stf + (long long)s * 3 * c.nt + (it - 1);
@@ -438,7 +661,7 @@ __global__ void __launch_bounds__(128) k_inject(const Consts c, float *__restric
     if (m & 2) fy = fy - d * S[c.nt];
     if (m & 4) fz = fz - d * S[2 * c.nt];
   }
-  F[0] = fx; F[N] = fy; F[2 * N] = fz;
+  F[0] = fx; F[125] = fy; F[250] = fz;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -510,6 +733,27 @@ __global__ void k_derive(const float *__restrict__ raw, float *__restrict__ mat,
     gm[G_KAPPA * N + q] = kappa;
     gm[G_QQ * N + q] = QQ;
   }
+}
+
+// Material coefficients from the reference layout (NMAT x N, element index fastest) into
+// element blocks [E][NMAT][128] (nodes 125..127 zero).
+__global__ void k_pack_mat(const float *__restrict__ ref, float *__restrict__ out, long long E) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= E * ELEM_MAT) return;
+  const long long e = q / ELEM_MAT;
+  const int r = (int)(q - e * ELEM_MAT), f = r / MAT_ROW, n = r % MAT_ROW;
+  out[q] = n < 125 ? ref[(long long)f * E * 125 + (long long)n * E + e] : 0.f;
+}
+
+// One state field of one event between the element-blocked state and the reference layout.
+__global__ void k_state_field(float *__restrict__ state_ev, int field, float *__restrict__ ref, long long E, int to_ref) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // reference index
+  if (q >= E * 125) return;
+  const long long e = q % E;
+  const int n = (int)(q / E);
+  float *sp = state_ev + (e * NSTATE + field) * 125 + n;
+  if (to_ref) ref[q] = *sp;
+  else *sp = ref[q];
 }
 
 // Mass matrix (SOURCE/ses3d_init.f90:254-279): each global node sums its element
@@ -592,8 +836,51 @@ static cudaError_t launch_elem_epb(int epb, const Consts &c, const Ptrs &p, cuda
   }
 }
 
+// Resident CTAs of k_element_tma<DISS, MODE> on the current device (set by prepare_tma).
+template <bool DISS, int MODE>
+static int &tma_grid_cap() {
+  static int cap = 0;
+  return cap;
+}
+template <bool DISS, int MODE>
+static cudaError_t prepare_tma() {
+  cudaError_t e = cudaFuncSetAttribute(k_element_tma<DISS, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)TMA_SMEM);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_element_tma<DISS, MODE>, TPE, TMA_SMEM);
+  if (e != cudaSuccess) return e;
+  tma_grid_cap<DISS, MODE>() = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  return cudaSuccess;
+}
+// Sets the shared-memory limit and grid size of the persistent element kernels; called
+// when a handle is created, before any stream capture.
+cudaError_t prepare_element_kernels() {
+  cudaError_t e;
+  if ((e = prepare_tma<false, 0>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<false, 3>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<true, 0>()) != cudaSuccess) return e;
+  return prepare_tma<true, 3>();
+}
+
+template <bool DISS, int MODE>
+static cudaError_t launch_tma(const Consts &c, const Ptrs &p, cudaStream_t st) {
+  const int grid_cap = tma_grid_cap<DISS, MODE>();
+  if (grid_cap <= 0) return cudaErrorInitializationError;
+  const long long total = c.E * (long long)c.nev;
+  const unsigned blocks = (unsigned)(total < grid_cap ? total : grid_cap);
+  k_element_tma<DISS, MODE><<<blocks, TPE, TMA_SMEM, st>>>(c, p);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_element(int diss, int mode, int epb, const Consts &c, const Ptrs &p, cudaStream_t st) {
   if (mode == 0 && c.lean) mode = 3;
+  if (epb <= 1 && (mode == 0 || mode == 3)) {  // persistent TMA-pipelined kernel
+    if (diss) return mode == 3 ? launch_tma<true, 3>(c, p, st) : launch_tma<true, 0>(c, p, st);
+    return mode == 3 ? launch_tma<false, 3>(c, p, st) : launch_tma<false, 0>(c, p, st);
+  }
   if (diss) {
     if (mode == 1) return launch_elem_epb<true, 1>(epb, c, p, st);
     if (mode == 2) return launch_elem_epb<true, 2>(epb, c, p, st);
@@ -647,6 +934,18 @@ cudaError_t launch_derive(const float *raw, float *mat, float *gm, long long N, 
 cudaError_t launch_mass(const Consts &c, const float *rhoinv, const float *z, const float *sinx, const float *w,
                         float Jac, float *MM, float *iMM, cudaStream_t st) {
   k_mass<<<(unsigned)((c.G + 255) / 256), 256, 0, st>>>(c, rhoinv, z, sinx, w, Jac, MM, iMM);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_mat(const float *ref, float *out, long long E, cudaStream_t st) {
+  const long long n = E * ELEM_MAT;
+  k_pack_mat<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ref, out, E);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_state_field(float *state_ev, int field, float *ref, long long E, int to_ref, cudaStream_t st) {
+  const long long n = E * 125;
+  k_state_field<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(state_ev, field, ref, E, to_ref);
   return cudaGetLastError();
 }
 

@@ -7,8 +7,8 @@ namespace ses3d {
 
 constexpr int TPE = 128;  // threads per element (125 GLL nodes + 3 idle lanes)
 
-// Element-local state, per event: 36 SoA fields of N floats, element-major
-// ([element][125 nodes], node n = in + 5 jn + 25 kn).
+// Element-local state, element-blocked: [event][element][36 fields][125 nodes] (node
+// n = in + 5 jn + 25 kn), i.e. the 36 fields of one element are 18,000 contiguous bytes.
 enum StateField {
   F_SXX = 0, F_SYY, F_SZZ, F_SXY, F_SYX, F_SXZ, F_SZX, F_SYZ, F_SZY,        // PML-split stresses
   F_DXUX = 9, F_DYUY, F_DZUZ, F_DXUY, F_DYUX, F_DXUZ, F_DZUX, F_DYUZ, F_DZUY, // displacement gradients
@@ -16,8 +16,12 @@ enum StateField {
   NSTATE = 36
 };
 
-// Per-node material coefficients (element-major), derived once from the model.
+// Per-node material coefficients, element-blocked with 128-float rows:
+// [element][6 fields][128] (nodes 125..127 zero), 3,072 bytes per element.
 enum MatField { M_CLAM = 0, M_C2MUT, M_C2MT, M_A, M_B2, M_C, NMAT };
+constexpr int ELEM_STATE = NSTATE * 125;  // floats of one element's state
+constexpr int MAT_ROW = 128;
+constexpr int ELEM_MAT = NMAT * MAT_ROW;  // floats of one element's material block
 // Adjoint-only per-node quantities.
 enum GMatField { G_RHO = 0, G_CP, G_CS, G_MU, G_KAPPA, G_QQ, NGMAT };
 // Forward record fields (the ffd files of the reference).
@@ -56,12 +60,13 @@ struct Ptrs {
   const float *pxg, *pyg, *pzg;         // raw PML per global index (last writer)
   const float *MM;                      // [G]
   const float *iMM;                     // [G] 1 / MM
-  const float *mat;                     // [NMAT][N]
-  const float *gmat;                    // [NGMAT][N] (adjoint)
-  float *state;                         // [nev][NSTATE][N]
+  const float *mat;                     // [E][NMAT][128]
+  const float *gmat;                    // [NGMAT][E][125] (adjoint)
+  float *state;                         // [nev][E][NSTATE][125]
   float *v;                             // [nev][3][G]
-  float *f;                             // [nev][3][N] element-local forces (scratch)
+  float *f;                             // [nev][E][3][125] element-local forces (scratch)
   int *d_it;                            // completed iterations
+  int *err;                             // device error word (bounded waits that gave up)
   // moment-tensor source per event
   const int *src_elem;                  // [nev], -1: none
   const float *src_delta;               // [nev][125]
