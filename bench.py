@@ -178,12 +178,13 @@ def run_ours(args, rank, world, local):
     ex, ey, ez = p.nx + 1, p.ny + 1, p.nz + 1
     G = (4 * ex + 1) * (4 * ey + 1) * (4 * ez + 1)
     r_u = G / N
-    # lean stepping: displacement gradients only in PML elements (outputs unchanged)
+    # lean stepping: displacement gradients and mirror stresses only in PML elements
+    # (outputs unchanged)
     E = ex * ey * ez
     pml = p.pml
     n_pml_el = E - max(0, ex - 2 * pml) * max(0, ey - 2 * pml) * max(0, ez - pml)
     interior_frac = 0.0 if not args.lean else (E - n_pml_el) / E
-    DU_B = 72.0  # 9 displacement gradients read + written
+    DU_B = 96.0  # 9 displacement gradients + 3 mirror stresses, read + written
     sim = Simulation.from_problem(p)
     sim.set_lean(args.lean)
     if args.epb:
@@ -301,6 +302,8 @@ def run_ours(args, rank, world, local):
         res["e2e"] = e2e
     if not args.no_batched:
         res["batched"] = run_batched(args, world)
+    if rank == 0 and world == 1 and not args.no_grad:
+        res["gradient"] = run_gradient(args)
     if rank == 0 and world == 1 and not args.no_cpu:
         res["cpu_baseline"] = cpu_baseline(p, args.cpu_steps)
     return res
@@ -337,6 +340,55 @@ def run_batched(args, world):
                         "CUDA graph of 10 iterations" % (n, min(nrec), max(nrec)),
             "events": 16, "ms_per_step": ms16, "value": world * 16 * n / (ms16 / 1e3), "unit": METRIC,
             "single_event_ms_per_step": ms1, "per_event_speedup_vs_single": 16 * ms1 / ms16}
+
+
+def gradient_once(workload, nt, nev, seed, truth_kind):
+    """One misfit gradient through the public autograd API (waveform_misfit forward +
+    backward: forward run with records or checkpoints, misfit, adjoint sources, adjoint run,
+    kernel readout), timed end to end. Observed data come from a perturbed model (untimed)."""
+    import numpy as np
+    import torch
+    from ses3d_gb300 import adjoint as A
+    from ses3d_gb300 import synth
+    p = synth.make_problem(workload, nt=nt, seed=seed, n_events=nev, adjoint_flag=1)
+    setup = A.MisfitSetup.from_problem(p, samp_ad=10)
+    m0 = A.problem_tensors(p)
+    if truth_kind == "blob":    # +-5 % vs Gaussian blob, radius 150 km at 200 km depth
+        truth = synth.build_model(p.box, blob=(0.05, 150e3, 200e3), is_diss=1)
+    else:                       # +-4 % vs checkerboard, 200 km cells
+        truth = synth.build_model(p.box, checker=(0.04, 200e3), is_diss=1)
+    setup.set_observed(A.problem_tensors(synth.Problem(p.setup, p.box, p.tau, p.D, truth, p.events, pml=p.pml)))
+    ms = [t.clone().requires_grad_(True) for t in m0]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    chi = A.waveform_misfit(setup, *ms)
+    chi.backward()
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    finite = bool(all(torch.isfinite(t.grad).all() for t in ms)) and bool(np.isfinite(float(chi.detach())))
+    nrec = [len(e.receivers.names) for e in p.events]
+    info = {"events": nev, "nt": nt, "samp_ad": 10, "gll_points_per_event": p.n_nodes,
+            "receivers_per_event": [min(nrec), max(nrec)],
+            "records_per_checkpoint_segment": setup.last.get("records_per_segment", 0),
+            "seconds": sec, "s_per_event_gradient": sec / nev, "finite": finite}
+    del setup, ms, chi
+    torch.cuda.empty_cache()
+    return info
+
+
+def run_gradient(args):
+    """'s per event gradient': the 64x64x32 single-event gradient of the misfit workload at
+    its full length, and batched (16 events in one handle) against single-event gradients on
+    the 48x48x24 mesh over a shorter run."""
+    out = {"api": "ses3d_gb300.adjoint.waveform_misfit forward + backward (torch.autograd)",
+           "dtype": "f32 fields, f64 kernel and misfit accumulation"}
+    out["single_64x64x32"] = gradient_once("c3", args.grad_nt, 1, args.seed, "blob")
+    one = gradient_once("c4", args.grad_batched_nt, 1, args.seed, "checker")
+    many = gradient_once("c4", args.grad_batched_nt, 16, args.seed, "checker")
+    out["single_48x48x24"] = one
+    out["batched_48x48x24"] = many
+    out["batched_per_event_speedup_vs_single"] = one["s_per_event_gradient"] / many["s_per_event_gradient"]
+    return out
 
 
 def run_reference(args, rank, world):
@@ -386,6 +438,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--lean", type=int, default=1, help="1: displacement gradients only in PML elements")
     ap.add_argument("--batched-steps", type=int, default=40)
+    ap.add_argument("--no-grad", action="store_true")
+    ap.add_argument("--grad-nt", type=int, default=4000, help="time steps of the 64x64x32 gradient")
+    ap.add_argument("--grad-batched-nt", type=int, default=200, help="time steps of the 48x48x24 gradients")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

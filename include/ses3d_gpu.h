@@ -161,6 +161,12 @@ enum {
  * research Q kernels of SOURCE/ses3d_grad_Q.f90 (normalised after the last step). */
 int ses3d_gpu_get_kernel(ses3d_gpu *h, int event, int which, double *out);
 
+/* Sum over all events of one kernel (FP64, events added in index order on the device),
+ * N doubles in the reference layout: the multi-event misfit gradient. The reference runs
+ * one event per job and sums the grad_* files afterwards; this returns that sum with one
+ * transfer. */
+int ses3d_gpu_get_kernel_sum(ses3d_gpu *h, int which, double *out);
+
 /* Forward-field records kept in device memory by an adjoint_flag == 1 run: one
  * record per stored iteration (it == 1, it % samp_ad == 0, it == nt), 9 fields of
  * N floats each: vx, vy, vz, exx, eyy, ezz, exy, exz, eyz -- the fields and order of
@@ -237,10 +243,12 @@ int ses3d_gpu_kernel_time(const ses3d_gpu *h, int which, double *total_ms, int64
  * The caller owns the wavefield and passes it in device memory:
  *   state: n_events x E x 36 x 125 floats (16-byte aligned) -- per event and element
  *          (i + ex (j + ey k)) a block of 36 fields of 125 nodes (in + 5 jn + 25 kn), the
- *          fields in the order sxx, syy, szz, sxy, syx, sxz, szx, syz, szy (PML
+ *          fields in the order sxx, syy, szz, sxy, sxz, syz, syx, szx, szy (PML
  *          stresses), dxux, dyuy, dzuz, dxuy, dyux, dxuz, dzux, dyuz, dzuy, then the
  *          memory variables Mxx, Myy, Mzz, Mxy, Mxz, Myz with the mechanism fastest
- *          (fields 18-35 unused when is_diss = 0);
+ *          (fields 18-35 unused when is_diss = 0); with lean stepping on, elements
+ *          outside the PML keep only the first six stresses and the memory variables
+ *          up to date;
  *   v:     n_events x 3 x G floats -- assembled velocity, component-major, global node
  *          gx + GX (gy + GY gz), GX = 4 ex + 1, GY = 4 ey + 1.
  * Zeroed buffers start a run at rest. Model, sources, receivers and the step counter
@@ -257,13 +265,15 @@ int ses3d_gpu_kernel_time(const ses3d_gpu *h, int which, double *total_ms, int64
  * routine is called. */
 int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int n);
 
-/* Lean plain-forward stepping (adjoint_flag 0 only; off by default). The displacement
- * gradients dxux..dzuy enter a forward run only through the PML strain terms
- * (SOURCE/ses3d_evolution.f90:123-134), which vanish outside the PML; with lean stepping
- * they are read and written only in PML elements, which removes 72 of the 318 bytes the
- * element kernel moves per GLL point elsewhere. Seismograms, velocities, stresses and
- * memory variables are unchanged bit for bit; SES3D_FIELD_DXUX..DZUY of non-PML elements
- * then keep their last values instead of being integrated. */
+/* Lean plain-forward stepping (adjoint_flag 0 only; off by default). Outside the PML
+ * all profiles vanish, so (SOURCE/ses3d_evolution.f90:123-134,208-219) the displacement
+ * gradients dxux..dzuy enter no output and the mirror stresses syx, szx, szy stay equal
+ * to sxy, sxz, syz. With lean stepping, elements outside the PML read and write neither:
+ * 96 of the 318 bytes the element kernel moves per GLL point there. Seismograms,
+ * velocities, stresses and memory variables are unchanged bit for bit: the mirror
+ * stresses are brought up to date before any field transfer and when lean stepping is
+ * switched off; SES3D_FIELD_DXUX..DZUY of non-PML elements keep their last values
+ * instead of being integrated. begin_adjoint switches lean stepping off. */
 int ses3d_gpu_set_lean(ses3d_gpu *h, int enable);
 
 /* Element-kernel block shape: elements per CTA (1, 2 or 4); 0 selects the default.

@@ -1,6 +1,6 @@
 """Command-line runner.
 
-  python -m ses3d_gb300 run --workload c4 --events 1 --steps 10 [--epb 1] [--graph 0]
+  python -m ses3d_gb300 run --workload c4 --events 1 --steps 10 [--epb 1] [--graph 0] [--lean 0]
       generates a seeded workload in memory and runs it on cuda:0, printing the
       per-iteration time (used for profiling captures and quick checks);
   python -m ses3d_gb300 generate --workload c1 --out DIR [--nt 1000]
@@ -21,6 +21,7 @@ def main(argv=None):
     r.add_argument("--steps", type=int, default=10)
     r.add_argument("--epb", type=int, default=1)
     r.add_argument("--graph", type=int, default=0)
+    r.add_argument("--lean", type=int, default=0, help="1: lean plain-forward stepping")
     r.add_argument("--seed", type=int, default=1234)
     r.add_argument("--adjoint", action="store_true", help="forward with records, then adjoint with kernels")
     g = sub.add_parser("generate")
@@ -43,6 +44,8 @@ def main(argv=None):
     p = synth.make_problem(a.workload, nt=a.steps + 2, seed=a.seed, n_events=a.events)
     sim = Simulation.from_problem(p, adjoint_flag=1 if a.adjoint else None)
     sim.set_block_elements(a.epb)
+    if a.lean:
+        sim.set_lean(True)
     if a.graph:
         sim.use_graph(True, a.graph)
     sim.step(1)

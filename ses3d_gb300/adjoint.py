@@ -249,7 +249,7 @@ class _Misfit:
                 dev = Q.device
                 grads = []
                 for name in ("rho", "cp", "csh", "csv", "Q_mu"):
-                    g = sum(sim.kernel(name, k) for k in range(sim.n_events)) * W * scale
+                    g = sim.kernel_sum(name) * W * scale
                     grads.append(torch.from_numpy(g).to(dev))
                 grads[4] = grads[4] / Q.double()
                 setup.last["kernels"] = {n: g for n, g in zip(("rho", "vp", "vsh", "vsv", "Q"), grads)}

@@ -29,6 +29,8 @@ cudaError_t launch_vmax(const float *v, long long G3, int nev, unsigned int *out
 cudaError_t launch_grad_q_norm(const Consts &c, const float *gm, double *grad, cudaStream_t st);
 cudaError_t launch_gather_ref(const Consts &c, const float *v, float *out, cudaStream_t st);
 cudaError_t prepare_element_kernels();
+cudaError_t launch_sync_mirrors(const Consts &c, float *state, cudaStream_t st);
+cudaError_t launch_sum_events_d(const double *grad, int slot, int nev, long long N, double *out, cudaStream_t st);
 cudaError_t launch_pack_mat(const float *ref, float *out, long long E, cudaStream_t st);
 cudaError_t launch_state_field(float *state_ev, int field, float *ref, long long E, int to_ref, cudaStream_t st);
 }  // namespace ses3d
@@ -83,6 +85,7 @@ struct ses3d_gpu {
   float *d_state = nullptr, *d_v = nullptr, *d_f = nullptr;
   int *d_it = nullptr;
   int *d_err = nullptr;  // device error word (bounded waits)
+  bool mirrors_stale = false;  // lean iterations left the mirror stresses outside the PML behind
   int *d_src_elem = nullptr;
   float *d_src_delta = nullptr, *d_src_mom = nullptr, *d_stf = nullptr;
   int *d_src_none = nullptr;  // all -1: no moment source (adjoint iterations)
@@ -317,6 +320,7 @@ int zero_wavefield(ses3d_gpu *h) {
   CK(h, cudaMemsetAsync(h->d_f, 0, nev * 3 * h->geo.N * sizeof(float), h->st));
   CK(h, cudaMemsetAsync(h->d_it, 0, sizeof(int), h->st));
   if (h->d_seis) CK(h, cudaMemsetAsync(h->d_seis, 0, (size_t)3 * h->cfg.nt * h->R * sizeof(float), h->st));
+  h->mirrors_stale = false;
   h->it = 0;
   return SES3D_OK;
 }
@@ -749,6 +753,15 @@ int ses3d_gpu_set_adjoint_sources(ses3d_gpu *h, int event, int n, const float *l
   return rebuild_forces(h);
 }
 
+// Brings the mirror stresses outside the PML up to date after lean iterations.
+static int sync_mirrors(ses3d_gpu *h) {
+  if (!h->mirrors_stale) return SES3D_OK;
+  CK(h, launch_sync_mirrors(h->c, h->d_state, h->st));
+  ++h->launches;
+  h->mirrors_stale = false;
+  return SES3D_OK;
+}
+
 // Reads and clears the device error word after the stream has drained.
 static int check_device_error(ses3d_gpu *h) {
   int err = 0;
@@ -817,6 +830,7 @@ int ses3d_gpu_step(ses3d_gpu *h, int n) {
       ++h->launches;
     }
   }
+  if (done > 0 && h->c.lean) h->mirrors_stale = true;
   CK(h, cudaStreamSynchronize(h->st));
   collect_times(h);
   return check_device_error(h);
@@ -878,6 +892,7 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
     if (e != cudaSuccess) return done(cuda_fail(h, e, "copy"));
   } else if (state_field_index(field) >= 0) {
     const int f = state_field_index(field);
+    if (int r = sync_mirrors(h)) return done(r);
     cudaError_t e;
     if (hout) {
       e = launch_state_field(sbase, f, tmp, h->geo.E, 1, h->st);
@@ -940,6 +955,25 @@ int ses3d_gpu_get_kernel(ses3d_gpu *h, int event, int which, double *out) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
   dfree(tmp);
   if (e != cudaSuccess) return cuda_fail(h, e, "get_kernel");
+  return SES3D_OK;
+}
+
+int ses3d_gpu_get_kernel_sum(ses3d_gpu *h, int which, double *out) {
+  if (!h) return SES3D_E_CONFIG;
+  if (which < 0 || which >= SES3D_KERNEL_COUNT || !out) return fail(h, SES3D_E_CONFIG, "bad kernel id");
+  if (!h->d_grad) return fail(h, SES3D_E_STATE, "kernels exist only in adjoint runs (adjoint_flag = 2)");
+  const long long N = h->geo.N;
+  double *tmp = nullptr, *sum = nullptr;
+  CK(h, dalloc(&tmp, (size_t)N));
+  cudaError_t e = dalloc(&sum, (size_t)N);
+  if (e == cudaSuccess) e = launch_sum_events_d(h->d_grad, which, h->cfg.n_events, N, sum, h->st);
+  if (e == cudaSuccess) e = launch_transpose_d(sum, tmp, h->geo.E, NPE, h->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, tmp, N * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  dfree(tmp);
+  dfree(sum);
+  if (e != cudaSuccess) return cuda_fail(h, e, "get_kernel_sum");
+  h->launches += 2;
   return SES3D_OK;
 }
 
@@ -1009,6 +1043,7 @@ int ses3d_gpu_begin_adjoint(ses3d_gpu *h) {
   if (!h) return SES3D_E_CONFIG;
   h->mode_flag = 2;
   h->cfg.adjoint_flag = 2;
+  h->c.lean = 0;  // lean stepping is a plain-forward mode; the wavefield is zeroed below
   if (!h->d_grad) {
     CK(h, dalloc(&h->d_grad, (size_t)h->cfg.n_events * NGRAD * h->geo.N));
   }
@@ -1170,6 +1205,11 @@ int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
 int ses3d_gpu_set_lean(ses3d_gpu *h, int enable) {
   if (!h) return SES3D_E_CONFIG;
   if (enable && h->mode_flag != 0) return fail(h, SES3D_E_CONFIG, "lean stepping applies to plain forward runs only");
+  if (!enable) {
+    int rc = sync_mirrors(h);
+    if (rc) return rc;
+    CK(h, cudaStreamSynchronize(h->st));
+  }
   h->c.lean = enable ? 1 : 0;
   destroy_graph(h);
   return SES3D_OK;

@@ -19,7 +19,10 @@
 #endif
 // The same for k_node (256-thread CTAs).
 #ifndef SES3D_NODE_MINB
-#define SES3D_NODE_MINB 4
+#define SES3D_NODE_MINB 6
+#endif
+#ifndef SES3D_NODE_TX
+#define SES3D_NODE_TX 0
 #endif
 
 namespace ses3d {
@@ -31,7 +34,7 @@ namespace ses3d {
 // element forces. Shared by both element kernels (one barrier inside).
 // ---------------------------------------------------------------------------------------
 struct ElemCtx {
-  bool act, keep_du;
+  bool act, full;
   int n, nn, in, jn, kn, ii, j, k, ev;
   unsigned e;
   size_t N, m0;
@@ -39,11 +42,17 @@ struct ElemCtx {
   float vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC;
 };
 
+// Element forces: component c of node n of element e at 375 e + 125 c + n of its event.
+__device__ __forceinline__ unsigned force_offset(const Consts &c, int i, int j, int k, int in, int jn, int kn) {
+  return ((unsigned)i + (unsigned)c.ex * ((unsigned)j + (unsigned)c.ey * (unsigned)k)) * 375u +
+         (unsigned)(in + 5 * jn + 25 * kn);
+}
+
 template <bool DISS, int MODE>
 __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, const KTab &tab, float (*s_v)[TPE],
                                                 float (*s_p)[TPE], const ElemCtx &x, float *sv) {
   constexpr int NS = DISS ? NSTATE : 18;
-  const bool act = x.act, keep_du = x.keep_du;
+  const bool act = x.act, full = x.full;
   const int n = x.n, nn = x.nn, in = x.in, jn = x.jn, kn = x.kn, ii = x.ii, j = x.j, k = x.k, ev = x.ev;
   const unsigned e = x.e;
   const size_t N = x.N, m0 = x.m0;
@@ -91,7 +100,7 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
     const float dxuy = sv[F_DXUY] + dt * exy, dyux = sv[F_DYUX] + dt * eyx;
     const float dxuz = sv[F_DXUZ] + dt * exz, dzux = sv[F_DZUX] + dt * ezx;
     const float dyuz = sv[F_DYUZ] + dt * eyz, dzuy = sv[F_DZUY] + dt * ezy;
-    if (keep_du) {
+    if (full) {
       S[F_DXUX * 125] = dxux; S[F_DYUY * 125] = dyuy; S[F_DZUZ * 125] = dzuz;
       S[F_DXUY * 125] = dxuy; S[F_DYUX * 125] = dyux; S[F_DXUZ * 125] = dxuz;
       S[F_DZUX * 125] = dzux; S[F_DYUZ * 125] = dyuz; S[F_DZUY * 125] = dzuy;
@@ -172,8 +181,8 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
     s_zy = s_zy + dt * (syz - pz * s_zy);
     // taper (ses3d_evolution.f90:368-371); the divergence below uses the untapered values
     S[F_SXX * 125] = s_xx * taper; S[F_SYY * 125] = s_yy * taper; S[F_SZZ * 125] = s_zz * taper;
-    S[F_SXY * 125] = s_xy * taper; S[F_SYX * 125] = s_yx * taper; S[F_SXZ * 125] = s_xz * taper;
-    S[F_SZX * 125] = s_zx * taper; S[F_SYZ * 125] = s_yz * taper; S[F_SZY * 125] = s_zy * taper;
+    S[F_SXY * 125] = s_xy * taper; S[F_SXZ * 125] = s_xz * taper; S[F_SYZ * 125] = s_yz * taper;
+    if (full) { S[F_SYX * 125] = s_yx * taper; S[F_SZX * 125] = s_zx * taper; S[F_SZY * 125] = s_zy * taper; }
     // moment-tensor source field (ses3d_miscellaneous.f90:115-147)
     if (MODE != 2 && (int)e == __ldg(p.src_elem + ev)) {
       const int it = *p.d_it + 1;
@@ -261,7 +270,7 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
       az2 = fmaf(s_p[8][iz], dzq, az2);
     }
     const float cx = tab.CX[jn][kn] * r, cy = tab.CY[in][kn] * r, cz = tab.CZ[in][jn] * st;
-    float *F = p.f + ((size_t)ev * c.E + e) * 375 + nn;
+    float *F = p.f + (size_t)ev * 3 * N + force_offset(c, ii, j, k, in, jn, kn);
     F[0] = cx * ax0 + cy * ay0 + cz * az0;
     F[125] = cx * ax1 + cy * ay1 + cz * az1;
     F[250] = cx * ax2 + cy * ay2 + cz * az2;
@@ -302,7 +311,7 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
   constexpr int NS = DISS ? NSTATE : 18;  // elastic runs carry no memory variables
   // Outside the PML the displacement gradients enter no output of a plain forward run
   // (ses3d_evolution.f90:123-134 multiplies them by zero profiles); lean runs skip them there.
-  const bool keep_du =
+  const bool full =
       MODE != 3 || i < c.pml || i >= c.ex - c.pml || j < c.pml || j >= c.ey - c.pml || k >= c.ez - c.pml;
   float sv[NS];
   float clam = 0.f, c2mut = 0.f, c2mt = 0.f, cA = 0.f, cB2 = 0.f, cC = 0.f;
@@ -330,11 +339,12 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
     const float *v = p.v + (size_t)ev * 3 * c.G + g;
     vx = v[0]; vy = v[c.G]; vz = v[2 * c.G];
 #pragma unroll
-    for (int f = 0; f < F_DXUX; ++f) sv[f] = S[f * 125];
-    if (keep_du) {
+    for (int f = 0; f < F_SYX; ++f) sv[f] = S[f * 125];
+    if (full) {
 #pragma unroll
-      for (int f = F_DXUX; f <= F_DZUY; ++f) sv[f] = S[f * 125];
-    } else {  // lean stepping outside the PML
+      for (int f = F_SYX; f <= F_DZUY; ++f) sv[f] = S[f * 125];
+    } else {  // lean stepping outside the PML: mirrors from their partners, no gradients
+      sv[F_SYX] = sv[F_SXY]; sv[F_SZX] = sv[F_SXZ]; sv[F_SZY] = sv[F_SYZ];
 #pragma unroll
       for (int f = F_DXUX; f <= F_DZUY; ++f) sv[f] = 0.f;
     }
@@ -349,7 +359,7 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
   }
   s_v[sub][0][n] = vx; s_v[sub][1][n] = vy; s_v[sub][2][n] = vz;
   __syncthreads();
-  ElemCtx x{act, keep_du, n, nn, in, jn, kn, ii, j, k, ev, e, N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC};
+  ElemCtx x{act, full, n, nn, in, jn, kn, ii, j, k, ev, e, N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC};
   element_compute<DISS, MODE>(c, p, tab, s_v[sub], s_p[sub], x, sv);
 }
 
@@ -358,19 +368,34 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
 // k_element_tma: persistent element kernel for plain and lean forward iterations. Each
 // 128-thread CTA walks (element, event) items with a stride of the grid; one thread copies
 // an item's whole state block (18,000 B) and material block (3,072 B) into shared memory
-// with cp.async.bulk on an mbarrier, two items ahead of the compute, so the loads leave the
-// register file and overlap the previous item's arithmetic. Results equal k_element's bit
+// with cp.async.bulk on an mbarrier, ahead of the compute (the next item's copy is issued
+// as soon as the current one has been read into registers), so the loads leave the
+// register file and overlap the current item's arithmetic. Results equal k_element's bit
 // for bit (same arithmetic, only the source of the loaded values differs).
 // Every mbarrier wait is bounded (2 s of %globaltimer): on expiry the block records an
 // error in p.err, waits (bounded again) for its copies still in flight and returns; the
 // host reports the failed step.
 // ---------------------------------------------------------------------------------------
-constexpr int TMA_STAGES = 2;
+// Shape of k_element_tma (measured on the 96 x 96 x 40 mesh): one state stage refilled as
+// soon as it has been read, at most 102 registers (5 CTAs per SM), and the element-local
+// velocity gathered one item ahead with cp.async.
+#ifndef SES3D_TMA_STAGES
+#define SES3D_TMA_STAGES 1
+#endif
+#ifndef SES3D_TMA_MINB
+#define SES3D_TMA_MINB 5
+#endif
+#ifndef SES3D_TMA_VPREF
+#define SES3D_TMA_VPREF 1
+#endif
+constexpr int TMA_STAGES = SES3D_TMA_STAGES;
+constexpr int TMA_VBUF = SES3D_TMA_VPREF ? 2 : 1;  // element-local velocity buffers
 struct __align__(16) ElemStage {
   float state[ELEM_STATE];  // 18,000 B
   float mat[ELEM_MAT];      // 3,072 B
 };
-constexpr size_t TMA_BAR_OFF = TMA_STAGES * sizeof(ElemStage) + 12 * TPE * sizeof(float) + ((sizeof(KTab) + 15) / 16) * 16;
+constexpr size_t TMA_BAR_OFF =
+    TMA_STAGES * sizeof(ElemStage) + (9 + 3 * TMA_VBUF) * TPE * sizeof(float) + ((sizeof(KTab) + 15) / 16) * 16;
 constexpr size_t TMA_SMEM = TMA_BAR_OFF + TMA_STAGES * sizeof(unsigned long long);
 
 __device__ __forceinline__ unsigned smem_addr(const void *ptr) { return (unsigned)__cvta_generic_to_shared(ptr); }
@@ -426,8 +451,8 @@ __device__ __forceinline__ bool in_pml_element(const Consts &c, int i, int j, in
 
 // Copies of one item into a stage. Byte ranges (element block of 18,000 B, fields of 500 B):
 // all 36 fields; elastic: fields 0-17 (9,008 B, the last 8 B inside field 18); lean outside
-// the PML: fields 0-8 (4,512 B) and, with attenuation, 18-35 (from byte 8,992, 9,008 B),
-// skipping the displacement gradients. Every range starts and ends 16-B aligned inside the block.
+// the PML: fields 0-5 (3,008 B) and, with attenuation, 18-35 (from byte 8,992, 9,008 B),
+// skipping the mirror stresses and the displacement gradients. Every range starts and ends 16-B aligned inside the block.
 template <bool DISS, int MODE>
 __device__ __forceinline__ void issue_item(const Consts &c, const Ptrs &p, long long item, ElemStage *st,
                                            unsigned long long *bar) {
@@ -440,14 +465,14 @@ __device__ __forceinline__ void issue_item(const Consts &c, const Ptrs &p, long 
   char *dst = reinterpret_cast<char *>(st->state);
   constexpr unsigned MB = ELEM_MAT * sizeof(float);
   if (!DISS && MODE == 3 && !in_pml_element(c, i, j, k)) {
-    mbar_arrive_expect_tx(bar, 4512u + MB);
-    bulk_g2s(dst, src, 4512u, bar);
+    mbar_arrive_expect_tx(bar, 3008u + MB);
+    bulk_g2s(dst, src, 3008u, bar);
   } else if (!DISS) {
     mbar_arrive_expect_tx(bar, 9008u + MB);
     bulk_g2s(dst, src, 9008u, bar);
   } else if (MODE == 3 && !in_pml_element(c, i, j, k)) {
-    mbar_arrive_expect_tx(bar, 4512u + 9008u + MB);
-    bulk_g2s(dst, src, 4512u, bar);
+    mbar_arrive_expect_tx(bar, 3008u + 9008u + MB);
+    bulk_g2s(dst, src, 3008u, bar);
     bulk_g2s(dst + 8992, src + 8992, 9008u, bar);
   } else {
     mbar_arrive_expect_tx(bar, (unsigned)(ELEM_STATE * sizeof(float)) + MB);
@@ -456,12 +481,31 @@ __device__ __forceinline__ void issue_item(const Consts &c, const Ptrs &p, long 
   bulk_g2s(st->mat, msrc, MB, bar);
 }
 
+// Element-local velocity of one item gathered from the assembled field straight into
+// shared memory with 4-byte cp.async (ses3d_evolution.f90:27-51); one commit group.
+__device__ __forceinline__ void gather_v_async(const Consts &c, const Ptrs &p, long long item, float (*dst)[TPE], int n,
+                                               int in, int jn, int kn) {
+  if (n < 125) {
+    const int ev = (int)(item % c.nev);
+    const unsigned e = (unsigned)(item / c.nev);
+    const int i = (int)(e % (unsigned)c.ex), j = (int)((e / (unsigned)c.ex) % (unsigned)c.ey);
+    const int k = (int)(e / ((unsigned)c.ex * (unsigned)c.ey));
+    const size_t g = (size_t)(i * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
+    const float *v = p.v + (size_t)ev * 3 * c.G + g;
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(&dst[q][n])), "l"(v + (size_t)q * c.G)
+                   : "memory");
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
 template <bool DISS, int MODE>
-__global__ void __launch_bounds__(TPE, 4) k_element_tma(const Consts c, const Ptrs p) {
+__global__ void __launch_bounds__(TPE, SES3D_TMA_MINB) k_element_tma(const Consts c, const Ptrs p) {
   extern __shared__ __align__(128) unsigned char smem[];
   ElemStage *stage = reinterpret_cast<ElemStage *>(smem);
-  float (*s_v)[TPE] = reinterpret_cast<float (*)[TPE]>(smem + TMA_STAGES * sizeof(ElemStage));
-  float (*s_p)[TPE] = s_v + 3;
+  float (*s_vb)[TPE] = reinterpret_cast<float (*)[TPE]>(smem + TMA_STAGES * sizeof(ElemStage));  // [TMA_VBUF][3]
+  float (*s_p)[TPE] = s_vb + 3 * TMA_VBUF;
   KTab *tab = reinterpret_cast<KTab *>(s_p + 9);
   unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + TMA_BAR_OFF);
 
@@ -483,19 +527,24 @@ __global__ void __launch_bounds__(TPE, 4) k_element_tma(const Consts c, const Pt
   const bool on = n < 125;
   const int nn = on ? n : 0;
   const int in = nn % 5, jn = (nn / 5) % 5, kn = nn / 25;
+  if (TMA_VBUF == 2 && first < total) gather_v_async(c, p, first, s_vb, n, in, jn, kn);
   for (int t = 0;; ++t) {
     const long long item = first + (long long)t * stride;
     if (item >= total) break;
     const int s = t % TMA_STAGES;
     const unsigned parity = (unsigned)(t / TMA_STAGES) & 1u;
+    float (*s_v)[TPE] = s_vb + 3 * (t % TMA_VBUF);
     const int ev = (int)(item % c.nev);
     const unsigned e = (unsigned)(item / c.nev);
     const int i = (int)(e % (unsigned)c.ex), j = (int)((e / (unsigned)c.ex) % (unsigned)c.ey);
     const int k = (int)(e / ((unsigned)c.ex * (unsigned)c.ey));
-    const bool keep_du = MODE != 3 || in_pml_element(c, i, j, k);
-    // gather v_global -> element-local v (ses3d_evolution.f90:27-51), issued before the wait
+    const bool full = MODE != 3 || in_pml_element(c, i, j, k);
     float vx = 0.f, vy = 0.f, vz = 0.f;
-    if (on) {
+    if (TMA_VBUF == 2) {  // this item's velocity was gathered one item ahead
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      if (on) { vx = s_v[0][n]; vy = s_v[1][n]; vz = s_v[2][n]; }
+    } else if (on) {
+      // gather v_global -> element-local v (ses3d_evolution.f90:27-51), issued before the wait
       const size_t g = (size_t)(i * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
       const float *v = p.v + (size_t)ev * 3 * c.G + g;
       vx = v[0]; vy = v[c.G]; vz = v[2 * c.G];
@@ -507,11 +556,12 @@ __global__ void __launch_bounds__(TPE, 4) k_element_tma(const Consts c, const Pt
       const float *ss = stage[s].state + nn;
       const float *sm = stage[s].mat + nn;
 #pragma unroll
-      for (int f = 0; f < F_DXUX; ++f) sv[f] = ss[f * 125];
-      if (keep_du) {
+      for (int f = 0; f < F_SYX; ++f) sv[f] = ss[f * 125];
+      if (full) {
 #pragma unroll
-        for (int f = F_DXUX; f <= F_DZUY; ++f) sv[f] = ss[f * 125];
-      } else {
+        for (int f = F_SYX; f <= F_DZUY; ++f) sv[f] = ss[f * 125];
+      } else {  // lean stepping outside the PML: mirrors from their partners, no gradients
+        sv[F_SYX] = sv[F_SXY]; sv[F_SZX] = sv[F_SXZ]; sv[F_SZY] = sv[F_SYZ];
 #pragma unroll
         for (int f = F_DXUX; f <= F_DZUY; ++f) sv[f] = 0.f;
       }
@@ -524,15 +574,18 @@ __global__ void __launch_bounds__(TPE, 4) k_element_tma(const Consts c, const Pt
 #pragma unroll
       for (int f = 0; f < NS; ++f) sv[f] = 0.f;
     }
-    s_v[0][n] = vx; s_v[1][n] = vy; s_v[2][n] = vz;
-    if (__syncthreads_or(!ok)) {  // a copy never arrived: drain both stages, then leave
+    if (TMA_VBUF == 1) { s_v[0][n] = vx; s_v[1][n] = vy; s_v[2][n] = vz; }
+    if (__syncthreads_or(!ok)) {  // a copy never arrived: drain the stages, then leave
       if (n == 0) {
         mbar_wait_bounded(&bar[s], parity, p.err);
-        if (item + stride < total) mbar_wait_bounded(&bar[s ^ 1], (unsigned)((t + 1) / TMA_STAGES) & 1u, p.err);
+        if constexpr (TMA_STAGES == 2)
+          if (item + stride < total) mbar_wait_bounded(&bar[s ^ 1], (unsigned)((t + 1) / TMA_STAGES) & 1u, p.err);
       }
       return;
     }
-    // stage s fully read, s_v complete
+    // stage s fully read, s_v complete; the other velocity buffer was last read before the
+    // previous item's divergence barrier
+    if (TMA_VBUF == 2 && item + stride < total) gather_v_async(c, p, item + stride, s_vb + 3 * ((t + 1) % 2), n, in, jn, kn);
     if (n == 0) {
       const long long next = item + TMA_STAGES * stride;
       if (next < total) {
@@ -542,7 +595,7 @@ __global__ void __launch_bounds__(TPE, 4) k_element_tma(const Consts c, const Pt
     }
     const size_t m0 = (size_t)e * 125 + nn;
     float *S = p.state + ((size_t)ev * c.E + e) * ELEM_STATE + nn;
-    ElemCtx x{on, keep_du, n, nn, in, jn, kn, i, j, k, ev, e, (size_t)c.N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC};
+    ElemCtx x{on, full, n, nn, in, jn, kn, i, j, k, ev, e, (size_t)c.N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC};
     element_compute<DISS, (MODE == 3 ? 3 : 0)>(c, p, *tab, s_v, s_p, x, sv);
   }
 }
@@ -554,14 +607,25 @@ __global__ void __launch_bounds__(TPE, 4) k_element_tma(const Consts c, const Pt
 // (ses3d_evolution.f90:318-328,366).
 // ---------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256, SES3D_NODE_MINB) k_node(const Consts c, const Ptrs p) {
-  const unsigned t = blockIdx.x * 256u + threadIdx.x;
   const int gz = blockIdx.y, ev = blockIdx.z;
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
     *p.d_it += 1;  // every reader of the counter ran earlier in stream order
   const unsigned GXY = (unsigned)c.GX * (unsigned)c.GY;
+#if SES3D_NODE_TX
+  // CTA = NODE_TX x (256 / NODE_TX) tile of (gx, gy): the rows of one element's forces that
+  // neighbouring gy read come through the same L1
+  constexpr int TY = 256 / SES3D_NODE_TX;
+  const unsigned tiles_x = ((unsigned)c.GX + SES3D_NODE_TX - 1) / SES3D_NODE_TX;
+  const int gx = (int)((blockIdx.x % tiles_x) * SES3D_NODE_TX + threadIdx.x % SES3D_NODE_TX);
+  const int gy = (int)((blockIdx.x / tiles_x) * TY + threadIdx.x / SES3D_NODE_TX);
+  if (gx >= c.GX || gy >= c.GY) return;
+  const unsigned t = (unsigned)gx + (unsigned)c.GX * (unsigned)gy;
+#else
+  const unsigned t = blockIdx.x * 256u + threadIdx.x;
   if (t >= GXY) return;
   const int gy = (int)(t / (unsigned)c.GX);
   const int gx = (int)t - gy * c.GX;
+#endif
   const size_t g = (size_t)gz * GXY + t;
   // node-local loads first: they do not depend on the element forces
   float *V = p.v + (size_t)ev * 3 * c.G + g;
@@ -571,16 +635,29 @@ __global__ void __launch_bounds__(256, SES3D_NODE_MINB) k_node(const Consts c, c
   const int i0 = gx == 0 ? 0 : (gx - 1) >> 2, i1 = min(gx >> 2, c.ex - 1);
   const int j0 = gy == 0 ? 0 : (gy - 1) >> 2, j1 = min(gy >> 2, c.ey - 1);
   const int k0 = gz == 0 ? 0 : (gz - 1) >> 2, k1 = min(gz >> 2, c.ez - 1);
-  const float *F = p.f + (size_t)ev * 3 * (size_t)c.N;  // [E][3][125]; 3 N < 2^32 is checked at create
+  const float *F = p.f + (size_t)ev * 3 * (size_t)c.N;  // 3 N < 2^32 is checked at create
+  // all (up to 8) contributions are loaded first, then summed in the reference order;
+  // the offset of contribution (i, j, k) is the sum of one term per axis (see force_offset)
+  const unsigned sy_ = (unsigned)c.ex * 375u, sz_ = sy_ * (unsigned)c.ey;
+  const unsigned ox[2] = {(unsigned)i0 * 371u + (unsigned)gx, (unsigned)i1 * 371u + (unsigned)gx};  // 375 i + gx - 4 i
+  const unsigned oy[2] = {(unsigned)j0 * (sy_ - 20u) + 5u * (unsigned)gy, (unsigned)j1 * (sy_ - 20u) + 5u * (unsigned)gy};
+  const unsigned oz[2] = {(unsigned)k0 * (sz_ - 100u) + 25u * (unsigned)gz, (unsigned)k1 * (sz_ - 100u) + 25u * (unsigned)gz};
+  const bool ux = i1 != i0, uy = j1 != j0, uz = k1 != k0;
+  float fx[8], fy[8], fz[8];
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const bool use = (!(a & 4) || ux) && (!(a & 2) || uy) && (!(a & 1) || uz);
+    fx[a] = fy[a] = fz[a] = 0.f;
+    if (use) {
+      const unsigned q = ox[(a >> 2) & 1] + oy[(a >> 1) & 1] + oz[a & 1];
+      fx[a] = F[q]; fy[a] = F[q + 125]; fz[a] = F[q + 250];
+    }
+  }
   float sx = 0.f, sy = 0.f, sz = 0.f;
-  for (int i = i0; i <= i1; ++i) {
-    const unsigned xi = (unsigned)i * 375u + (unsigned)(gx - 4 * i);
-    for (int j = j0; j <= j1; ++j)
-      for (int k = k0; k <= k1; ++k) {
-        const unsigned q = xi + (unsigned)c.ex * ((unsigned)j + (unsigned)c.ey * (unsigned)k) * 375u +
-                           (unsigned)(5 * (gy - 4 * j) + 25 * (gz - 4 * k));
-        sx += F[q]; sy += F[q + 125]; sz += F[q + 250];
-      }
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const bool use = (!(a & 4) || ux) && (!(a & 2) || uy) && (!(a & 1) || uz);
+    if (use) { sx += fx[a]; sy += fy[a]; sz += fz[a]; }
   }
   // a = s / MM with the reciprocal of the mass matrix (ses3d_evolution.f90:318-320)
   const float ax = sx * imm, ay = sy * imm, az = sz * imm;
@@ -651,7 +728,8 @@ __global__ void __launch_bounds__(128) k_inject(const Consts c, float *__restric
   if (n >= 125) return;
   const int it = *d_it + 1;
   const long long N = c.N;
-  float *F = f + ((long long)gr.x * c.E + gr.y) * 375 + n;  // [event][element][3][125]
+  const int e = gr.y, i = e % c.ex, j = (e / c.ex) % c.ey, k = e / (c.ex * c.ey);
+  float *F = f + (long long)gr.x * 3 * N + force_offset(c, i, j, k, n % 5, (n / 5) % 5, n / 25);
   float fx = F[0], fy = F[125], fz = F[250];
   for (int s = gr.z; s < gr.w; ++s) {
     const float d = delta[(long long)s * 125 + n];
@@ -754,6 +832,23 @@ __global__ void k_state_field(float *__restrict__ state_ev, int field, float *__
   float *sp = state_ev + (e * NSTATE + field) * 125 + n;
   if (to_ref) ref[q] = *sp;
   else *sp = ref[q];
+}
+
+// Mirror stresses of the elements outside the PML from their partners (syx = sxy,
+// szx = sxz, szy = syz there), after lean iterations that left them out.
+__global__ void k_sync_mirrors(const Consts c, float *__restrict__ state) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (event, element, node)
+  if (q >= (long long)c.nev * c.E * 125) return;
+  const long long el = q / 125;
+  const int n = (int)(q - el * 125);
+  const unsigned e = (unsigned)(el % c.E);
+  const int i = (int)(e % (unsigned)c.ex), j = (int)((e / (unsigned)c.ex) % (unsigned)c.ey);
+  const int k = (int)(e / ((unsigned)c.ex * (unsigned)c.ey));
+  if (in_pml_element(c, i, j, k)) return;
+  float *S = state + el * ELEM_STATE + n;
+  S[F_SYX * 125] = S[F_SXY * 125];
+  S[F_SZX * 125] = S[F_SXZ * 125];
+  S[F_SZY * 125] = S[F_SYZ * 125];
 }
 
 // Mass matrix (SOURCE/ses3d_init.f90:254-279): each global node sums its element
@@ -894,7 +989,13 @@ cudaError_t launch_element(int diss, int mode, int epb, const Consts &c, const P
 }
 
 cudaError_t launch_node(const Consts &c, const Ptrs &p, cudaStream_t st) {
+#if SES3D_NODE_TX
+  constexpr int TY = 256 / SES3D_NODE_TX;
+  dim3 grid((unsigned)((c.GX + SES3D_NODE_TX - 1) / SES3D_NODE_TX) * (unsigned)((c.GY + TY - 1) / TY), (unsigned)c.GZ,
+            (unsigned)c.nev);
+#else
   dim3 grid((unsigned)(((long long)c.GX * c.GY + 255) / 256), (unsigned)c.GZ, (unsigned)c.nev);
+#endif
   k_node<<<grid, 256, 0, st>>>(c, p);
   return cudaGetLastError();
 }
@@ -916,6 +1017,21 @@ cudaError_t launch_inject(const Consts &c, float *f, const int4 *groups, int ngr
 cudaError_t launch_transpose(const float *in, float *out, long long rows, long long cols, cudaStream_t st) {
   dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
   k_transpose<<<grid, dim3(32, 8), 0, st>>>(in, out, rows, cols);
+  return cudaGetLastError();
+}
+
+// Sum over events of one kernel slot, events in index order (deterministic).
+__global__ void k_sum_events_d(const double *__restrict__ grad, int slot, int nev, long long N,
+                               double *__restrict__ out) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= N) return;
+  double s = 0.0;
+  for (int ev = 0; ev < nev; ++ev) s += grad[((long long)ev * NGRAD + slot) * N + q];
+  out[q] = s;
+}
+
+cudaError_t launch_sum_events_d(const double *grad, int slot, int nev, long long N, double *out, cudaStream_t st) {
+  k_sum_events_d<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(grad, slot, nev, N, out);
   return cudaGetLastError();
 }
 
@@ -946,6 +1062,12 @@ cudaError_t launch_pack_mat(const float *ref, float *out, long long E, cudaStrea
 cudaError_t launch_state_field(float *state_ev, int field, float *ref, long long E, int to_ref, cudaStream_t st) {
   const long long n = E * 125;
   k_state_field<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(state_ev, field, ref, E, to_ref);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sync_mirrors(const Consts &c, float *state, cudaStream_t st) {
+  const long long n = (long long)c.nev * c.E * 125;
+  k_sync_mirrors<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(c, state);
   return cudaGetLastError();
 }
 

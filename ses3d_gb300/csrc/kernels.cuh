@@ -9,8 +9,11 @@ constexpr int TPE = 128;  // threads per element (125 GLL nodes + 3 idle lanes)
 
 // Element-local state, element-blocked: [event][element][36 fields][125 nodes] (node
 // n = in + 5 jn + 25 kn), i.e. the 36 fields of one element are 18,000 contiguous bytes.
+// Outside the PML all profiles vanish and the three mirror stresses (syx, szx, szy) stay
+// equal to their partners (sxy, sxz, syz); they are stored last of the nine so that lean
+// stepping can leave them out as one range.
 enum StateField {
-  F_SXX = 0, F_SYY, F_SZZ, F_SXY, F_SYX, F_SXZ, F_SZX, F_SYZ, F_SZY,        // PML-split stresses
+  F_SXX = 0, F_SYY, F_SZZ, F_SXY, F_SXZ, F_SYZ, F_SYX, F_SZX, F_SZY,        // PML-split stresses
   F_DXUX = 9, F_DYUY, F_DZUZ, F_DXUY, F_DYUX, F_DXUZ, F_DZUX, F_DYUZ, F_DZUY, // displacement gradients
   F_M = 18,  // memory variables: F_M + 3*comp + mech, comp = xx, yy, zz, xy, xz, yz
   NSTATE = 36

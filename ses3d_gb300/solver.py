@@ -192,6 +192,12 @@ class Simulation:
         self._check(self.lib.ses3d_gpu_get_kernel(self.h, event, L.KERNEL_ID[name], L.dptr(out)))
         return out
 
+    def kernel_sum(self, name: str) -> np.ndarray:
+        """Sum of one kernel over all events (summed on the device in event order)."""
+        out = np.zeros(self.N, np.float64)
+        self._check(self.lib.ses3d_gpu_get_kernel_sum(self.h, L.KERNEL_ID[name], L.dptr(out)))
+        return out
+
     def record_count(self, event: int = 0) -> int:
         return self._check(self.lib.ses3d_gpu_record_count(self.h, event))
 

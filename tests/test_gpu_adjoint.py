@@ -131,3 +131,23 @@ def test_q_kernels(runs, name):
     o64 = runs["o_kernels64"][name]
     assert np.abs(o64).max() > 0
     assert rel(g, o64) <= 1e-3, (name, rel(g, o64))
+
+
+def test_kernel_sum_over_events(native):
+    """ses3d_gpu_get_kernel_sum equals the per-event kernels added in event order."""
+    from ses3d_gb300.solver import Simulation
+    p = synth.make_problem("tiny", nt=NT, seed=37, adjoint_flag=1, n_events=3)
+    p.setup.samp_ad = SAMP
+    for k, e in enumerate(p.events):
+        e.event.zzs = np.float32(5000.0 + 6000.0 * k)
+    with Simulation.from_problem(p, adjoint_flag=1, grad_variant=1) as sim:
+        sim.run()
+        for k in range(3):
+            loc, stf = adjoint_inputs(p, sim.seismograms(k))
+            sim.set_adjoint_sources(k, loc, stf)
+        sim.begin_adjoint()
+        sim.run()
+        for name in ("rho", "csv", "Q_mu"):
+            per = [sim.kernel(name, k) for k in range(3)]
+            assert all(np.abs(a).max() > 0 for a in per)
+            assert np.array_equal(sim.kernel_sum(name), per[0] + per[1] + per[2]), name

@@ -202,6 +202,26 @@ def test_lean_stepping_changes_no_output(native):
         assert np.all(lean[name][~mask] == 0) and np.abs(full[name][~mask]).max() > 0
 
 
+def test_lean_switched_off_midway(native):
+    """Lean iterations followed by ordinary ones give the ordinary run bit for bit (the
+    mirror stresses outside the PML are brought up to date when lean stepping stops)."""
+    from ses3d_gb300.solver import Simulation
+    p = synth.make_problem("small", nt=60, seed=23)
+    outs = []
+    for mixed in (False, True):
+        with Simulation.from_problem(p) as sim:
+            if mixed:
+                sim.set_lean(True)
+                sim.use_graph(True, 10)
+                sim.step(30)
+                sim.set_lean(False)
+            sim.run()
+            outs.append([sim.field(k) for k in ("vx_global", "vy_global", "syx_pml", "szx_pml", "sxy_pml", "Mxz")] +
+                        [np.concatenate(sim.seismograms(0))])
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+
+
 def test_deterministic_repeat(native):
     from ses3d_gb300.solver import Simulation
     p = synth.make_problem("tiny", nt=30, seed=9)
