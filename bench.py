@@ -294,7 +294,8 @@ def run_ours(args, rank, world, local):
         "roofline": {"bound": "hbm", "kernel": "k_element", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes_per_launch": elem_bytes,
-                     "traffic": (tr or {}).get("dram_bytes_per_launch_full") if tr else None},
+                     "traffic": tr.get("dram_bytes_per_launch_full")
+                     if tr and bool(tr.get("lean")) == bool(args.lean) else None},
         "gpu_launches": launches,
         "clocks": clocks,
     }
