@@ -377,18 +377,74 @@ def gradient_once(workload, nt, nev, seed, truth_kind):
     return info
 
 
+def gradient_files_once(workload, nt, seed):
+    """One single-event gradient in the reference's own workflow, on this library: the
+    ses3d_gpu_main forward job (adjoint_flag 1) writes seismograms, forward-field records
+    and the saving vector to disk; the L2 adjoint sources are computed from the seismogram
+    files and written to ADJOINT/; the adjoint job (adjoint_flag 2) reads the records back
+    and writes the grad_* files, which are read. Same misfit, mesh and observed data as
+    gradient_once. The directory tree is written before the clock starts."""
+    import shutil
+    import numpy as np
+    from ses3d_gb300 import adjoint as A
+    from ses3d_gb300 import formats as F
+    from ses3d_gb300 import synth
+    p = synth.make_problem(workload, nt=nt, seed=seed, n_events=1, adjoint_flag=1)
+    p.setup.samp_ad = 10
+    setup = A.MisfitSetup.from_problem(p, samp_ad=10)
+    truth = synth.build_model(p.box, checker=(0.04, 200e3), is_diss=1)
+    setup.set_observed(A.problem_tensors(synth.Problem(p.setup, p.box, p.tau, p.D, truth, p.events, pml=p.pml)))
+    root = tempfile.mkdtemp(prefix="ses3d_grad_")
+    try:
+        synth.write_problem(p, root)
+        main = os.path.join(root, "MAIN")
+        driver = os.path.join(ROOT, "ses3d_gb300", "ses3d_gpu_main")
+        ev = p.events[0]
+        t0 = time.perf_counter()
+        subprocess.run([driver, "--main", main, "--pml", str(p.pml)], check=True, capture_output=True)
+        ofd = os.path.join(main, ev.event.ofd)
+        syn = np.stack([np.stack([F.read_seismogram(os.path.join(ofd, nm + "." + c))[2] for nm in ev.receivers.names])
+                        for c in "xyz"]).astype(np.float64)                     # (3, nr, nt)
+        srcs = setup.adjoint_sources([syn], float(ev.event.dt))[0]              # (nr, 3, nt)
+        adir = os.path.join(root, "ADJOINT", ev.name)
+        os.makedirs(adir, exist_ok=True)
+        loc = np.asarray(ev.receivers.loc, np.float32)
+        F.write_ad_srcfile(os.path.join(adir, "ad_srcfile"), loc)
+        for k in range(len(loc)):
+            F.write_ad_src(os.path.join(adir, "ad_src_%d" % (k + 1)), srcs[k], loc[k])
+        p.setup.adjoint_flag = 2
+        F.write_setup(os.path.join(root, "INPUT", "setup"), p.setup)
+        subprocess.run([driver, "--main", main, "--pml", str(p.pml)], check=True, capture_output=True)
+        grads = [F.read_record(os.path.join(ofd, "grad_%s_0" % nm), p.n_nodes) for nm in ("rho", "cp", "csh", "csv")]
+        sec = time.perf_counter() - t0
+        finite = all(bool(np.all(np.isfinite(g))) for g in grads)
+        ffd_bytes = sum(os.path.getsize(os.path.join(dp, f)) for dp, _, fs in os.walk(os.path.join(main, p.setup.ffd))
+                        for f in fs)
+    finally:
+        shutil.rmtree(root, ignore_errors=True)
+    return {"events": 1, "nt": nt, "samp_ad": 10, "gll_points_per_event": p.n_nodes,
+            "forward_record_bytes_on_disk": ffd_bytes, "disk": tempfile.gettempdir(),
+            "seconds": sec, "s_per_event_gradient": sec, "finite": finite}
+
+
 def run_gradient(args):
     """'s per event gradient': the 64x64x32 single-event gradient of the misfit workload at
     its full length, and batched (16 events in one handle) against single-event gradients on
-    the 48x48x24 mesh over a shorter run."""
+    the 48x48x24 mesh and on the small 22x22x10 mesh over a shorter run."""
     out = {"api": "ses3d_gb300.adjoint.waveform_misfit forward + backward (torch.autograd)",
            "dtype": "f32 fields, f64 kernel and misfit accumulation"}
     out["single_64x64x32"] = gradient_once("c3", args.grad_nt, 1, args.seed, "blob")
-    one = gradient_once("c4", args.grad_batched_nt, 1, args.seed, "checker")
-    many = gradient_once("c4", args.grad_batched_nt, 16, args.seed, "checker")
-    out["single_48x48x24"] = one
-    out["batched_48x48x24"] = many
-    out["batched_per_event_speedup_vs_single"] = one["s_per_event_gradient"] / many["s_per_event_gradient"]
+    for wl, tag in (("c4", "48x48x24"), ("c1", "22x22x10")):
+        one = gradient_once(wl, args.grad_batched_nt, 1, args.seed, "checker")
+        many = gradient_once(wl, args.grad_batched_nt, 16, args.seed, "checker")
+        out["single_" + tag] = one
+        out["batched_" + tag] = many
+        out["batched_per_event_speedup_vs_single_" + tag] = one["s_per_event_gradient"] / many["s_per_event_gradient"]
+        if wl == "c4":
+            files = gradient_files_once(wl, args.grad_batched_nt, args.seed)
+            out["single_files_" + tag] = files
+            out["batched_per_event_speedup_vs_single_files_" + tag] = (files["s_per_event_gradient"] /
+                                                                       many["s_per_event_gradient"])
     return out
 
 

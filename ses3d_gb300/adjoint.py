@@ -88,7 +88,7 @@ class MisfitSetup:
     fmin: float = 1.0 / 50.0
     fmax: float = 1.0 / 10.0
     samp_ad: int = 10
-    memory_budget: float = 150e9      # bytes for records/checkpoints of all events
+    memory_budget: Optional[float] = None  # bytes for records of all events; None: free device memory
     grad_q: bool = True
     last: dict = field(default_factory=dict)
 
@@ -130,6 +130,17 @@ class MisfitSetup:
         sim.run()
         return sim
 
+    def record_budget(self, sim: Simulation) -> float:
+        """Bytes available for forward records: memory_budget, or else the free device
+        memory less what the adjoint run allocates later (FP64 kernel accumulators, 64 B
+        per GLL point and event) and a reserve (5 % of the device, at least 8 GB)."""
+        if self.memory_budget is not None:
+            return float(self.memory_budget)
+        import torch
+        free, total = torch.cuda.mem_get_info()
+        grad_b = 64.0 * sim.N * sim.n_events
+        return max(0.0, float(free) - grad_b - max(8e9, 0.05 * float(total)))
+
     def segment_length(self, sim: Simulation) -> int:
         """0 (keep every record) if all records fit the budget, else the checkpoint segment
         length K that minimises checkpoint + segment memory."""
@@ -137,7 +148,7 @@ class MisfitSetup:
         nrec = len([it for it in range(1, nt + 1) if it % s == 0 or it == 1 or it == nt])
         rec_b = 9.0 * sim.N * 4 * sim.n_events
         ck_b = (36.0 * sim.N + 3.0 * sim.G) * 4 * sim.n_events
-        if nrec * rec_b <= self.memory_budget:
+        if nrec * rec_b <= self.record_budget(sim):
             return 0
         K = max(1, int(round(math.sqrt(nrec * ck_b / rec_b))))
         return K
