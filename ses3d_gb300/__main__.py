@@ -4,7 +4,12 @@
       generates a seeded workload in memory and runs it on cuda:0, printing the
       per-iteration time (used for profiling captures and quick checks);
   python -m ses3d_gb300 generate --workload c1 --out DIR [--nt 1000]
-      writes the workload as a reference directory tree (INPUT/, MODELS/MODELS/).
+      writes the workload as a reference directory tree (INPUT/, MODELS/MODELS/);
+  python -m ses3d_gb300 adjoint-sources --seismograms OFD --out ADJOINT/1 --kind cc
+          --component z --window 10 50 [--taper 5 | --freq 0.05] [--stations A B ...]
+          [--bandpass FMIN FMAX] [--integrate] [--depth METRES]
+      writes ad_srcfile and ad_src_<k> for the listed (default: all) stations from SES3D
+      seismogram files, one measurement per station (TOOLS/adjoint_source.py).
 """
 import argparse
 import json
@@ -29,7 +34,22 @@ def main(argv=None):
     g.add_argument("--out", required=True)
     g.add_argument("--nt", type=int, default=None)
     g.add_argument("--seed", type=int, default=1234)
+    q = sub.add_parser("adjoint-sources")
+    q.add_argument("--seismograms", required=True, help="directory holding <station>.{x,y,z}")
+    q.add_argument("--out", required=True)
+    q.add_argument("--kind", default="cc", choices=["cc", "L2amp", "mttime", "mtamp"])
+    q.add_argument("--component", default="z", choices=["x", "y", "z"])
+    q.add_argument("--window", type=float, nargs=2, required=True, metavar=("LEFT", "RIGHT"))
+    q.add_argument("--taper", type=float, default=None, help="cosine taper width [s] (cc, L2amp)")
+    q.add_argument("--freq", type=float, default=None, help="frequency [Hz] (mttime, mtamp)")
+    q.add_argument("--stations", nargs="*", default=None)
+    q.add_argument("--bandpass", type=float, nargs=2, default=None, metavar=("FMIN", "FMAX"))
+    q.add_argument("--integrate", action="store_true", help="integrate velocity to displacement first")
+    q.add_argument("--depth", type=float, default=None, help="adjoint source depth [m] (default: receiver's)")
     a = ap.parse_args(argv)
+
+    if a.cmd == "adjoint-sources":
+        return adjoint_sources_cmd(a)
 
     from . import synth
     if a.cmd == "generate":
@@ -62,6 +82,31 @@ def main(argv=None):
         out["adjoint_ms_per_step"] = (time.perf_counter() - t2) * 1e3 / (a.steps + 1)
     sim.close()
     print(json.dumps(out))
+    return 0
+
+
+def adjoint_sources_cmd(a):
+    import os
+    from . import adjoint_sources as AS
+    if a.kind in ("cc", "L2amp") and a.taper is None:
+        raise SystemExit("--taper is required for %s" % a.kind)
+    if a.kind in ("mttime", "mtamp") and a.freq is None:
+        raise SystemExit("--freq is required for %s" % a.kind)
+    names = a.stations
+    if not names:
+        names = sorted(f[:-2] for f in os.listdir(a.seismograms) if f.endswith(".x"))
+    sources = []
+    for nm in names:
+        s = AS.Seismogram().read(a.seismograms, nm, integrate=a.integrate)
+        if a.bandpass:
+            s.bandpass(*a.bandpass)
+        src = AS.AdjointSource()
+        src.fetch_seismogram(s)
+        arg = a.taper if a.kind in ("cc", "L2amp") else a.freq
+        getattr(src, "make_adsrc_" + a.kind)(a.component, a.window[0], a.window[1], arg)
+        sources.append(src)
+    AS.write_adjoint_directory(a.out, sources, depth=a.depth)
+    print(json.dumps({"adjoint_sources": len(sources), "kind": a.kind, "out": a.out}))
     return 0
 
 

@@ -114,3 +114,40 @@ def test_multibox_tree_is_rejected(native, tmp_path):
     F.write_boxfile(os.path.join(root, "MODELS", "MODELS", "boxfile"), F.make_boxes(s), 2, 1, 1)
     res = subprocess.run([DRIVER, "--main", os.path.join(root, "MAIN")], capture_output=True, text=True, timeout=120)
     assert res.returncode != 0 and "processor boxes" in res.stderr
+
+
+def test_adjoint_sources_tool_in_the_file_workflow(native, oracle_mod, tmp_path):
+    """Forward job -> seismogram files -> cross-correlation adjoint sources written by
+    `python -m ses3d_gb300 adjoint-sources` -> adjoint job -> grad_* files, against the
+    oracle run on the same records and adjoint sources."""
+    from ses3d_gb300.__main__ import main
+    nt = 60
+    p = synth.make_problem("tiny", nt=nt, seed=64, adjoint_flag=1)
+    p.setup.samp_ad = 5
+    p.setup.ffd = "../DATA/FFD"
+    root = str(tmp_path)
+    synth.write_problem(p, root)
+    run_driver(root, p.pml)
+    ev = p.events[0]
+    ofd = os.path.join(root, "MAIN", ev.event.ofd)
+    adir = os.path.join(root, "ADJOINT", ev.name)
+    assert main(["adjoint-sources", "--seismograms", ofd, "--out", adir, "--kind", "cc", "--component", "z",
+                 "--window", "0.5", "5.5", "--taper", "0.5", "--stations"] + list(ev.receivers.names)) == 0
+    loc = F.read_ad_srcfile(os.path.join(adir, "ad_srcfile"))
+    stf = np.stack([F.read_ad_src(os.path.join(adir, "ad_src_%d" % (k + 1)), nt) for k in range(len(loc))])
+    assert np.abs(stf).max() > 0
+    p.setup.adjoint_flag = 2
+    F.write_setup(os.path.join(root, "INPUT", "setup"), p.setup)
+    run_driver(root, p.pml)
+    o = oracle_mod.Oracle(p, adjoint_flag=1)
+    o.run(nt)
+    recs = np.stack([o.record(r) for r in range(o.nrecords())])
+    sv = o.get_int("saving_vector")[1:nt + 1]
+    oa = oracle_mod.Oracle(p, adjoint_flag=2, saving_vector=sv, ad_loc=loc, ad_stf=stf)
+    oa.set_records(recs)
+    oa.run(nt)
+    for nm in ("rho", "cp", "csh", "csv"):
+        g = F.read_record(os.path.join(ofd, "grad_%s_0" % nm), p.n_nodes)
+        ref = oa.get("grad_" + nm)
+        assert np.abs(ref).max() > 0
+        assert rel(g, ref) <= 1e-3, nm
