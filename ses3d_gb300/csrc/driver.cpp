@@ -6,7 +6,15 @@
 // writes seismograms, snapshots, forward fields, saving_vector and grad_* kernels in the
 // reference layouts (SOURCE/ses3d_output.f90).
 //
-//   ses3d_gpu_main [--main DIR] [--pml N] [--grad-q]
+// A boxfile of several processor boxes (px, py, pz > 1) is run as one mesh on the GPU:
+// the per-rank model files are stitched on input, and every per-rank output (snapshots
+// v?_<rank>_<it>, forward fields <name>_<rank>, saving_vector_<rank>, grad_*_<rank>) is
+// split back out, padded to the reference build's array extents nx_max, ny_max, nz_max
+// (--max-elements; default: the largest box). Seismograms are written once per receiver.
+//
+//   ses3d_gpu_main [--main DIR] [--pml N] [--grad-q] [--max-elements NX NY NZ]
+//                  [--stitch-model OUTDIR]
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -47,19 +55,96 @@ struct Args {
   std::string main = ".";
   int pml = 2;  // the reference's compile-time default (SOURCE/ses3d_modules.f90:21)
   int grad_q = 0;
+  int max_el[3] = {-1, -1, -1};  // nx_max, ny_max, nz_max of the reference build
+  std::string stitch_out;        // write the stitched single-box model there and stop
 };
+
+const char *kModelNames[7] = {"rhoinv", "mu", "lambda", "A", "B", "C", "Q"};
+
+// Boxfile -> decomposition with the build's array extents.
+bool load_decomposition(const Args &a, Decomposition &dec, std::string &err) {
+  int px, py, pz;
+  std::vector<BoxEntry> boxes;
+  if (!read_boxfile(join(a.main, "../MODELS/MODELS/boxfile"), px, py, pz, boxes, err)) return false;
+  if (!make_decomposition(boxes, px, py, pz, dec, err)) return false;
+  if (a.max_el[0] >= 0) {
+    if (a.max_el[0] < dec.pad_x || a.max_el[1] < dec.pad_y || a.max_el[2] < dec.pad_z) {
+      err = "--max-elements smaller than a processor box";
+      return false;
+    }
+    dec.pad_x = a.max_el[0]; dec.pad_y = a.max_el[1]; dec.pad_z = a.max_el[2];
+  }
+  return true;
+}
+
+// The union of the boxes as one box (physical bounds from the boxfile).
+BoxEntry union_box(const Decomposition &dec) {
+  BoxEntry u = dec.boxes[0];
+  for (const BoxEntry &b : dec.boxes) {
+    u.xmin = std::min(u.xmin, b.xmin); u.xmax = std::max(u.xmax, b.xmax);
+    u.ymin = std::min(u.ymin, b.ymin); u.ymax = std::max(u.ymax, b.ymax);
+    u.zmin = std::min(u.zmin, b.zmin); u.zmax = std::max(u.zmax, b.zmax);
+  }
+  u.index = 1; u.mx = u.my = u.mz = 1;
+  u.nx_min = 0; u.nx_max = dec.ex - 1; u.ny_min = 0; u.ny_max = dec.ey - 1; u.nz_min = 0; u.nz_max = dec.ez - 1;
+  return u;
+}
+
+// MODELS/MODELS/<name><rank> of every box (SOURCE/ses3d_input.f90:472-499), stitched.
+bool read_stitched_model(const Args &a, const Decomposition &dec, int k, std::vector<float> &out, std::string &err) {
+  out.assign(dec.global_points(), 0.0f);
+  for (size_t b = 0; b < dec.boxes.size(); ++b) {
+    std::vector<std::vector<float>> recs;
+    const std::string nm = std::string(kModelNames[k]) + std::to_string(dec.boxes[b].index - 1);
+    if (!read_records(join(a.main, "../MODELS/MODELS/" + nm), recs, err)) return false;
+    if (recs.empty() || recs[0].size() != dec.box_points(b, false)) {
+      err = "model record " + nm + " does not hold " + std::to_string(dec.box_points(b, false)) + " values";
+      return false;
+    }
+    dec.gather(b, recs[0].data(), false, out.data());
+  }
+  return true;
+}
+
+// One record per box: <prefix><rank><suffix>, padded to the build's extents.
+bool write_split(const Decomposition &dec, const std::string &prefix, const std::string &suffix, const float *global,
+                 bool append, std::string &err) {
+  std::vector<float> local;
+  for (size_t b = 0; b < dec.boxes.size(); ++b) {
+    local.resize(dec.box_points(b, true));
+    dec.scatter(b, global, true, local.data());
+    if (!write_record(prefix + std::to_string(dec.boxes[b].index - 1) + suffix, local.data(), local.size(), append, err))
+      return false;
+  }
+  return true;
+}
+
+// Stitched single-box copy of a multi-box model (boxfile + <name>0), no GPU needed.
+int stitch_model(const Args &a) {
+  std::string err;
+  Decomposition dec;
+  if (!load_decomposition(a, dec, err)) return die(err);
+  SetupFile su;
+  if (!read_setup(join(a.main, "../INPUT/setup"), su, err)) return die(err);
+  make_dirs(a.stitch_out);
+  for (int k = 0; k < 7; ++k) {
+    if (k == 6 && !su.is_diss) continue;
+    std::vector<float> g;
+    if (!read_stitched_model(a, dec, k, g, err)) return die(err);
+    if (!write_record(a.stitch_out + "/" + kModelNames[k] + "0", g.data(), g.size(), false, err)) return die(err);
+  }
+  if (!write_single_boxfile(a.stitch_out + "/boxfile", union_box(dec), err)) return die(err);
+  std::printf("stitched %zu boxes into %d x %d x %d elements\n", dec.boxes.size(), dec.ex, dec.ey, dec.ez);
+  return 0;
+}
 
 int run_event(const Args &a, const std::string &id) {
   std::string err;
   const std::string in = join(a.main, "../INPUT/");
   // ---- ses3d_input (SOURCE/ses3d_input.f90:44-618)
-  int px, py, pz;
-  std::vector<BoxEntry> boxes;
-  if (!read_boxfile(join(a.main, "../MODELS/MODELS/boxfile"), px, py, pz, boxes, err)) return die(err);
-  if (boxes.size() != 1 || px * py * pz != 1)
-    return die("the boxfile describes " + std::to_string(boxes.size()) +
-               " processor boxes; one GPU runs the whole mesh: regenerate the model with px = py = pz = 1");
-  const BoxEntry &b = boxes[0];
+  Decomposition dec;
+  if (!load_decomposition(a, dec, err)) return die(err);
+  const BoxEntry b = union_box(dec);
   EventFile ev;
   SetupFile su;
   float tau[3], D[3];
@@ -80,17 +165,12 @@ int run_event(const Args &a, const std::string &id) {
   make_dirs(ffd);
   ses3d_gpu *h = nullptr;
   if (api(ses3d_gpu_create(&cfg, &h), nullptr, "create") < 0) return 1;
-  const size_t N = (size_t)125 * (cfg.nx + 1) * (cfg.ny + 1) * (cfg.nz + 1);
-  // model records (SOURCE/ses3d_input.f90:472-499)
-  const char *mnames[7] = {"rhoinv", "mu", "lambda", "A", "B", "C", "Q"};
+  const size_t N = dec.global_points();
+  // model records (SOURCE/ses3d_input.f90:472-499), stitched over the processor boxes
   std::vector<std::vector<float>> model(7);
   for (int k = 0; k < 7; ++k) {
     if (k == 6 && !cfg.is_diss) continue;
-    std::vector<std::vector<float>> recs;
-    if (!read_records(join(a.main, std::string("../MODELS/MODELS/") + mnames[k] + "0"), recs, err)) return die(err);
-    if (recs.empty() || recs[0].size() != N)
-      return die(std::string("model record ") + mnames[k] + "0 does not hold " + std::to_string(N) + " values");
-    model[k] = std::move(recs[0]);
+    if (!read_stitched_model(a, dec, k, model[k], err)) return die(err);
   }
   if (api(ses3d_gpu_set_model(h, model[0].data(), model[1].data(), model[2].data(), model[3].data(), model[4].data(),
                               model[5].data(), cfg.is_diss ? model[6].data() : nullptr), h, "set_model") < 0)
@@ -116,17 +196,29 @@ int run_event(const Args &a, const std::string &id) {
   } else {
     // forward fields, read as the reference reads them back (SOURCE/ses3d_output.f90:172-267)
     std::vector<int> sv;
-    if (!read_saving_vector(ffd + "saving_vector_0", cfg.nt, sv, err)) return die(err);
-    std::vector<std::vector<std::vector<float>>> fields(9);
-    for (int f = 0; f < 9; ++f)
-      if (!read_records(ffd + kRecordNames[f] + "_0", fields[f], err)) return die(err);
-    const size_t nrec = fields[0].size();
+    if (!read_saving_vector(ffd + "saving_vector_" + std::to_string(dec.boxes[0].index - 1), cfg.nt, sv, err))
+      return die(err);
+    // per box and field all records of that file; stitched one record at a time
+    std::vector<std::vector<std::vector<std::vector<float>>>> fields(dec.boxes.size(),
+                                                                     std::vector<std::vector<std::vector<float>>>(9));
+    size_t nrec = 0;
+    for (size_t bx = 0; bx < dec.boxes.size(); ++bx)
+      for (int f = 0; f < 9; ++f) {
+        const std::string fn = ffd + kRecordNames[f] + "_" + std::to_string(dec.boxes[bx].index - 1);
+        if (!read_records(fn, fields[bx][f], err)) return die(err);
+        if (bx == 0 && f == 0) nrec = fields[0][0].size();
+        if (fields[bx][f].size() != nrec) return die("inconsistent forward-field records in " + fn);
+        for (const std::vector<float> &rr : fields[bx][f])
+          if (rr.size() != dec.box_points(bx, true) && rr.size() != dec.box_points(bx, false))
+            return die("forward-field record size in " + fn + " fits neither the box nor --max-elements");
+      }
     std::vector<float> one(9 * N);
     for (size_t r = 0; r < nrec; ++r) {
-      for (int f = 0; f < 9; ++f) {
-        if (fields[f].size() != nrec || fields[f][r].size() != N) return die("inconsistent forward-field records");
-        std::memcpy(&one[(size_t)f * N], fields[f][r].data(), N * sizeof(float));
-      }
+      for (size_t bx = 0; bx < dec.boxes.size(); ++bx)
+        for (int f = 0; f < 9; ++f) {
+          const std::vector<float> &rr = fields[bx][f][r];
+          dec.gather(bx, rr.data(), rr.size() == dec.box_points(bx, true), &one[(size_t)f * N]);
+        }
       if (api(ses3d_gpu_put_record(h, 0, (int)r, one.data()), h, "put_record") < 0) return 1;
     }
     fields.clear();
@@ -168,10 +260,10 @@ int run_event(const Args &a, const std::string &id) {
   };
   auto write_snapshot = [&](int it) -> bool {
     if (ev.output_displacement != 1) return true;
-    const char *nm[3] = {"vx_0_", "vy_0_", "vz_0_"};
+    const char *nm[3] = {"vx_", "vy_", "vz_"};
     for (int c = 0; c < 3; ++c) {
       if (api(ses3d_gpu_get_field(h, 0, SES3D_FIELD_VX + c, snap.data()), h, "get_field") < 0) return false;
-      if (!write_record(ofd + nm[c] + std::to_string(it), snap.data(), N, false, err)) { die(err); return false; }
+      if (!write_split(dec, ofd + nm[c], "_" + std::to_string(it), snap.data(), false, err)) { die(err); return false; }
     }
     return true;
   };
@@ -202,19 +294,20 @@ int run_event(const Args &a, const std::string &id) {
     for (int k = 0; k < 4; ++k) {
       if (api(ses3d_gpu_get_kernel(h, 0, SES3D_KERNEL_RHO + k, kd.data()), h, "get_kernel") < 0) return 1;
       for (size_t q = 0; q < N; ++q) kf[q] = (float)kd[q];
-      if (!write_record(ofd + kKernelNames[k] + "_0", kf.data(), N, false, err)) return die(err);
+      if (!write_split(dec, ofd + kKernelNames[k] + "_", "", kf.data(), false, err)) return die(err);
     }
   }
   if (cfg.adjoint_flag == 1) {
     std::vector<int> sv(cfg.nt);
     ses3d_gpu_get_saving_vector(h, sv.data());
-    if (!write_saving_vector(ffd + "saving_vector_0", sv, err)) return die(err);
+    for (const BoxEntry &bx : dec.boxes)  // every rank writes the same vector
+      if (!write_saving_vector(ffd + "saving_vector_" + std::to_string(bx.index - 1), sv, err)) return die(err);
     const int nrec = ses3d_gpu_record_count(h, 0);
     std::vector<float> one(9 * N);
     for (int r = 0; r < nrec; ++r) {  // ses3d_store records (SOURCE/ses3d_output.f90:138-162)
       if (api(ses3d_gpu_get_record(h, 0, r, one.data()), h, "get_record") < 0) return 1;
       for (int f = 0; f < 9; ++f)
-        if (!write_record(ffd + kRecordNames[f] + "_0", &one[(size_t)f * N], N, r > 0, err)) return die(err);
+        if (!write_split(dec, ffd + kRecordNames[f] + "_", "", &one[(size_t)f * N], r > 0, err)) return die(err);
     }
   }
   std::printf("event %s: %d iterations, %d receivers, %lld launches\n", id.c_str(), cfg.nt, nr,
@@ -236,14 +329,19 @@ int main(int argc, char **argv) {
     if (s == "--main") a.main = val("--main");
     else if (s == "--pml") a.pml = std::atoi(val("--pml").c_str());
     else if (s == "--grad-q") a.grad_q = 1;
+    else if (s == "--max-elements") {
+      for (int q = 0; q < 3; ++q) a.max_el[q] = std::atoi(val("--max-elements").c_str());
+    } else if (s == "--stitch-model") a.stitch_out = val("--stitch-model");
     else if (s == "-h" || s == "--help") {
-      std::printf("usage: ses3d_gpu_main [--main DIR] [--pml N] [--grad-q]\n");
+      std::printf("usage: ses3d_gpu_main [--main DIR] [--pml N] [--grad-q] [--max-elements NX NY NZ] "
+                  "[--stitch-model OUTDIR]\n");
       return 0;
     } else {
       std::fprintf(stderr, "unknown argument %s\n", s.c_str());
       return 2;
     }
   }
+  if (!a.stitch_out.empty()) return stitch_model(a);
   std::string err;
   std::vector<std::string> ids;
   if (!read_event_list(join(a.main, "../INPUT/event_list"), ids, err)) return die(err);

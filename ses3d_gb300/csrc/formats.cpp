@@ -3,6 +3,7 @@
 
 #include <sys/stat.h>
 
+#include <algorithm>
 #include <cerrno>
 #include <cmath>
 #include <cstdint>
@@ -205,6 +206,82 @@ bool read_boxfile(const std::string &path, int &px, int &py, int &pz, std::vecto
   return true;
 }
 
+bool make_decomposition(const std::vector<BoxEntry> &boxes, int px, int py, int pz, Decomposition &d,
+                        std::string &err) {
+  if (boxes.empty() || (size_t)px * py * pz != boxes.size()) {
+    err = "boxfile: " + std::to_string(boxes.size()) + " boxes for px * py * pz = " + std::to_string(px * py * pz);
+    return false;
+  }
+  d = Decomposition();
+  d.boxes = boxes;
+  for (const BoxEntry &b : boxes) {
+    if (b.mx < 1 || b.mx > px || b.my < 1 || b.my > py || b.mz < 1 || b.mz > pz || b.nx_max < b.nx_min ||
+        b.ny_max < b.ny_min || b.nz_max < b.nz_min) {
+      err = "boxfile: inconsistent box " + std::to_string(b.index);
+      return false;
+    }
+    d.ox.push_back(b.nx_min + b.mx - 1);
+    d.oy.push_back(b.ny_min + b.my - 1);
+    d.ex = std::max(d.ex, b.nx_max + b.mx);
+    d.ey = std::max(d.ey, b.ny_max + b.my);
+    d.ez = std::max(d.ez, b.nz_max + b.mz);
+    d.pad_x = std::max(d.pad_x, b.nx_max - b.nx_min);
+    d.pad_y = std::max(d.pad_y, b.ny_max - b.ny_min);
+    d.pad_z = std::max(d.pad_z, b.nz_max - b.nz_min);
+  }
+  // z: the boxfile counts upward (box mz = 1 at the bottom, SOURCE/ses3d_init.f90:600-611),
+  // element k downward from the top of each box (z = zmax - k dz, :238-242)
+  for (const BoxEntry &b : boxes) d.oz.push_back(d.ez - (b.nz_max + b.mz));
+  // every global element in exactly one box
+  std::vector<unsigned char> cover((size_t)d.ex * d.ey * d.ez, 0);
+  for (size_t q = 0; q < boxes.size(); ++q) {
+    const BoxEntry &b = boxes[q];
+    for (int k = 0; k <= b.nz_max - b.nz_min; ++k)
+      for (int j = 0; j <= b.ny_max - b.ny_min; ++j)
+        for (int i = 0; i <= b.nx_max - b.nx_min; ++i) {
+          unsigned char &c = cover[(size_t)(d.ox[q] + i) + (size_t)d.ex * ((d.oy[q] + j) + (size_t)d.ey * (d.oz[q] + k))];
+          if (c) { err = "boxfile: boxes overlap"; return false; }
+          c = 1;
+        }
+  }
+  for (unsigned char c : cover)
+    if (!c) { err = "boxfile: boxes leave elements uncovered"; return false; }
+  return true;
+}
+
+size_t Decomposition::box_points(size_t b, bool padded) const {
+  const BoxEntry &x = boxes[b];
+  const size_t lx = padded ? pad_x + 1 : x.nx_max - x.nx_min + 1, ly = padded ? pad_y + 1 : x.ny_max - x.ny_min + 1,
+               lz = padded ? pad_z + 1 : x.nz_max - x.nz_min + 1;
+  return 125 * lx * ly * lz;
+}
+
+namespace {
+template <bool TO_GLOBAL>
+void move_box(const Decomposition &d, size_t b, const float *src, bool padded, float *dst) {
+  const BoxEntry &x = d.boxes[b];
+  const int nx = x.nx_max - x.nx_min + 1, ny = x.ny_max - x.ny_min + 1, nz = x.nz_max - x.nz_min + 1;
+  const size_t lx = padded ? d.pad_x + 1 : nx, ly = padded ? d.pad_y + 1 : ny, lz = padded ? d.pad_z + 1 : nz;
+  for (int n = 0; n < 125; ++n)  // n = in + 5 jn + 25 kn, the slowest F-order index group
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j) {
+        const size_t lrow = lx * (j + ly * (k + lz * (size_t)n));
+        const size_t grow = (size_t)d.ox[b] + (size_t)d.ex * ((d.oy[b] + j) + (size_t)d.ey * ((d.oz[b] + k) + (size_t)d.ez * n));
+        if (TO_GLOBAL) std::memcpy(dst + grow, src + lrow, (size_t)nx * sizeof(float));
+        else std::memcpy(dst + lrow, src + grow, (size_t)nx * sizeof(float));
+      }
+}
+}  // namespace
+
+void Decomposition::gather(size_t b, const float *local, bool padded, float *global) const {
+  move_box<true>(*this, b, local, padded, global);
+}
+
+void Decomposition::scatter(size_t b, const float *global, bool padded, float *local) const {
+  std::fill(local, local + box_points(b, padded), 0.0f);
+  move_box<false>(*this, b, global, padded, local);
+}
+
 // SOURCE/ses3d_input.f90:594-598
 bool read_ad_srcfile(const std::string &path, std::vector<float> &loc, std::string &err) {
   LineReader r;
@@ -302,6 +379,30 @@ std::string fmt_int(long v) {
   char b[32];
   std::snprintf(b, sizeof(b), " %11ld", v);
   return b;
+}
+
+// Boxfile of one processor box, in the layout generate_models.f90 writes
+// (MODELS/SOURCE/generate_models.f90:285-330): 14 description lines, the process counts,
+// then the box entry.
+bool write_single_boxfile(const std::string &path, const BoxEntry &b, std::string &err) {
+  std::ofstream f(path);
+  if (!f) { err = "cannot write " + path; return false; }
+  const char *desc[14] = {" - format description -", " total number of processes", " number of processes in x direction",
+                          " number of processes in y direction", " number of processes in z direction",
+                          " single index (npz-1)*py*px+(npy-1)*px+npx", " multi index (npx, npy, npz)",
+                          " index boundaries x (x_min, x_max)", " index boundaries y (y_min, y_max)",
+                          " index boundaries z (z_min, z_max)", " physical boundaries x", " physical boundaries y",
+                          " phyiscal boundaries z", " -------------------"};
+  for (const char *d : desc) f << d << "\n";
+  f << fmt_int(1) << "\n" << fmt_int(1) << "\n" << fmt_int(1) << "\n" << fmt_int(1) << "\n";
+  f << " -------------------\n";
+  f << fmt_int(1) << "\n" << fmt_int(1) << fmt_int(1) << fmt_int(1) << "\n";
+  f << fmt_int(b.nx_min) << fmt_int(b.nx_max) << "\n" << fmt_int(b.ny_min) << fmt_int(b.ny_max) << "\n";
+  f << fmt_int(b.nz_min) << fmt_int(b.nz_max) << "\n";
+  f << fmt_real(b.xmin) << fmt_real(b.xmax) << "\n" << fmt_real(b.ymin) << fmt_real(b.ymax) << "\n";
+  f << fmt_real(b.zmin) << fmt_real(b.zmax) << "\n";
+  f << " -------------------\n";
+  return (bool)f;
 }
 
 // SOURCE/ses3d_output.f90:398-451

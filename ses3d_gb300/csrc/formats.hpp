@@ -53,6 +53,28 @@ struct BoxEntry {
   float xmin = 0, xmax = 0, ymin = 0, ymax = 0, zmin = 0, zmax = 0;
 };
 
+// Processor-box decomposition of a boxfile (SOURCE/ses3d_input.f90:44-170, boxes as
+// MODELS/SOURCE/generate_models.f90:200-283 writes them): box (mx, my, mz) holds the
+// global elements nx_min + mx - 1 .. nx_max + mx - 1 (likewise in y; in z the boxfile
+// counts upward while element k counts down from the top), so boxes are element-disjoint
+// and tile the mesh. Per-box arrays are the reference's F-order
+// (i, j, k, in, jn, kn) with element index fastest; `pad` gives the compile-time array
+// extents nx_max, ny_max, nz_max of the reference build (0:nx_max etc.), which its
+// snapshot, forward-field and kernel files are written with.
+struct Decomposition {
+  int ex = 0, ey = 0, ez = 0;                     // global element counts
+  std::vector<BoxEntry> boxes;
+  std::vector<int> ox, oy, oz;                    // global element offset of each box
+  int pad_x = 0, pad_y = 0, pad_z = 0;            // nx_max, ny_max, nz_max (>= every box's nx, ny, nz)
+  size_t global_points() const { return (size_t)125 * ex * ey * ez; }
+  size_t box_points(size_t b, bool padded) const;
+  // local (exact or padded) -> global, and global -> local (padding left zero)
+  void gather(size_t b, const float *local, bool padded, float *global) const;
+  void scatter(size_t b, const float *global, bool padded, float *local) const;
+};
+bool make_decomposition(const std::vector<BoxEntry> &boxes, int px, int py, int pz, Decomposition &d,
+                        std::string &err);
+
 struct Receivers {
   std::vector<std::string> names;  // 12 characters, blank padded
   std::vector<float> loc;          // 3 per receiver
@@ -81,6 +103,7 @@ bool write_seismogram_files(const std::string &ofd, const std::string &name12, c
                             const float *sz, int nt, float dt, const float recloc_deg[3], const float src_deg[3],
                             std::string &err);
 bool write_saving_vector(const std::string &path, const std::vector<int> &sv, std::string &err);
+bool write_single_boxfile(const std::string &path, const BoxEntry &b, std::string &err);
 bool make_dirs(const std::string &path);
 
 }  // namespace ses3d

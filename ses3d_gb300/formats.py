@@ -393,6 +393,46 @@ def make_boxes(s: Setup) -> List[Box]:
     return boxes
 
 
+def box_offsets(boxes: List[Box]):
+    """Global element counts (ex, ey, ez) of a decomposition and each box's global element
+    offset (ox, oy, oz). Box (mx, my, mz) starts at element nx_min + mx - 1 in x (and y);
+    the boxfile counts z upward (mz = 1 is the bottom box, SOURCE/ses3d_init.f90:600-611)
+    while element k counts down from the top (z = zmax - k dz), so oz = ez - nz_max - mz."""
+    ex = max(b.nx_max + b.multi[0] for b in boxes)
+    ey = max(b.ny_max + b.multi[1] for b in boxes)
+    ez = max(b.nz_max + b.multi[2] for b in boxes)
+    offs = [(b.nx_min + b.multi[0] - 1, b.ny_min + b.multi[1] - 1, ez - (b.nz_max + b.multi[2])) for b in boxes]
+    return (ex, ey, ez), offs
+
+
+def split_field(field: np.ndarray, boxes: List[Box], pad=None) -> List[np.ndarray]:
+    """Per-box pieces of a global element-local field (reference F-order, element index
+    fastest). pad = (nx_max, ny_max, nz_max) lays each piece out with the reference build's
+    array extents (0:nx_max, ...), zeros outside the box, as its output files are written."""
+    (ex, ey, ez), offs = box_offsets(boxes)
+    g = np.asarray(field).reshape(125, ez, ey, ex)
+    out = []
+    for b, (ox, oy, oz) in zip(boxes, offs):
+        piece = g[:, oz:oz + b.nz + 1, oy:oy + b.ny + 1, ox:ox + b.nx + 1]
+        if pad is not None:
+            full = np.zeros((125, pad[2] + 1, pad[1] + 1, pad[0] + 1), g.dtype)
+            full[:, :b.nz + 1, :b.ny + 1, :b.nx + 1] = piece
+            piece = full
+        out.append(np.ascontiguousarray(piece).reshape(-1))
+    return out
+
+
+def stitch_field(pieces: Sequence[np.ndarray], boxes: List[Box], pad=None) -> np.ndarray:
+    """Inverse of split_field."""
+    (ex, ey, ez), offs = box_offsets(boxes)
+    g = np.zeros((125, ez, ey, ex), np.asarray(pieces[0]).dtype)
+    for piece, b, (ox, oy, oz) in zip(pieces, boxes, offs):
+        dims = (pad[2] + 1, pad[1] + 1, pad[0] + 1) if pad is not None else (b.nz + 1, b.ny + 1, b.nx + 1)
+        a = np.asarray(piece).reshape(125, *dims)[:, :b.nz + 1, :b.ny + 1, :b.nx + 1]
+        g[:, oz:oz + b.nz + 1, oy:oy + b.ny + 1, ox:ox + b.nx + 1] = a
+    return g.reshape(-1)
+
+
 def write_boxfile(path: str, boxes: List[Box], px: int, py: int, pz: int):
     L = [" - format description -", " total number of processes", " number of processes in x direction",
          " number of processes in y direction", " number of processes in z direction",

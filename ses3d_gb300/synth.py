@@ -18,6 +18,7 @@ Workloads (element counts; lpd = 4):
 """
 from __future__ import annotations
 
+import copy
 import os
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional
@@ -320,8 +321,19 @@ def make_problem(name: str, seed: int = 1234, nt: Optional[int] = None, n_el=Non
     return Problem(setup, box, relax_tau, D, mdl, events, pml=pml, label=name)
 
 
-def write_problem(p: Problem, root: str):
-    """Writes the reference directory tree under root (INPUT/, MODELS/MODELS/, MAIN/)."""
+def split_setup(setup: F.Setup, n_el, procs) -> F.Setup:
+    """The setup of the same mesh decomposed into px x py x pz processor boxes
+    (nx_global = elements - px, INPUT/setup:11)."""
+    s = copy.deepcopy(setup)
+    s.px, s.py, s.pz = procs
+    s.nx_global, s.ny_global, s.nz_global = n_el[0] - procs[0], n_el[1] - procs[1], n_el[2] - procs[2]
+    return s
+
+
+def write_problem(p: Problem, root: str, procs=(1, 1, 1)):
+    """Writes the reference directory tree under root (INPUT/, MODELS/MODELS/, MAIN/);
+    procs = (px, py, pz) > 1 writes it decomposed into processor boxes the way the
+    reference's model generator does (per-rank model files, boxfile of all boxes)."""
     inp = os.path.join(root, "INPUT")
     os.makedirs(inp, exist_ok=True)
     os.makedirs(os.path.join(root, "MAIN"), exist_ok=True)
@@ -334,5 +346,15 @@ def write_problem(p: Problem, root: str):
         F.write_recfile(os.path.join(inp, "recfile_" + e.name), e.receivers)
     # the reference reads one stf file for every event (SOURCE/ses3d_input.f90:415)
     F.write_stf(os.path.join(inp, "stf"), p.events[0].stf, float(p.events[0].event.dt))
-    F.write_boxfile(os.path.join(root, "MODELS", "MODELS", "boxfile"), [p.box], 1, 1, 1)
-    F.write_model(os.path.join(root, "MODELS", "MODELS"), 0, p.model)
+    mdir = os.path.join(root, "MODELS", "MODELS")
+    if tuple(procs) == (1, 1, 1):
+        F.write_boxfile(os.path.join(mdir, "boxfile"), [p.box], 1, 1, 1)
+        F.write_model(mdir, 0, p.model)
+        return
+    s = split_setup(p.setup, (p.nx + 1, p.ny + 1, p.nz + 1), procs)
+    F.write_setup(os.path.join(inp, "setup"), s)
+    boxes = F.make_boxes(s)
+    F.write_boxfile(os.path.join(mdir, "boxfile"), boxes, *procs)
+    pieces = {k: F.split_field(v, boxes) for k, v in p.model.items()}
+    for r in range(len(boxes)):
+        F.write_model(mdir, r, {k: v[r] for k, v in pieces.items()})

@@ -105,15 +105,16 @@ def test_adjoint_round_trip_through_files(native, oracle_mod, tmp_path):
         assert rel(g, ref) <= 1e-3, nm
 
 
-def test_multibox_tree_is_rejected(native, tmp_path):
+def test_model_files_inconsistent_with_boxfile_are_rejected(native, tmp_path):
+    """A boxfile of two boxes over a single-box model: rank 0's model record has the wrong
+    size, which the driver reports before touching the GPU."""
     p = synth.make_problem("tiny", nt=5, seed=63)
     root = str(tmp_path)
     synth.write_problem(p, root)
-    s = p.setup
-    s.px = 2
+    s = synth.split_setup(p.setup, (p.nx + 1, p.ny + 1, p.nz + 1), (2, 1, 1))
     F.write_boxfile(os.path.join(root, "MODELS", "MODELS", "boxfile"), F.make_boxes(s), 2, 1, 1)
     res = subprocess.run([DRIVER, "--main", os.path.join(root, "MAIN")], capture_output=True, text=True, timeout=120)
-    assert res.returncode != 0 and "processor boxes" in res.stderr
+    assert res.returncode != 0 and "does not hold" in res.stderr
 
 
 def test_adjoint_sources_tool_in_the_file_workflow(native, oracle_mod, tmp_path):
