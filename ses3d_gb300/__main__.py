@@ -9,7 +9,12 @@
           --component z --window 10 50 [--taper 5 | --freq 0.05] [--stations A B ...]
           [--bandpass FMIN FMAX] [--integrate] [--depth METRES]
       writes ad_srcfile and ad_src_<k> for the listed (default: all) stations from SES3D
-      seismogram files, one measurement per station (TOOLS/adjoint_source.py).
+      seismogram files, one measurement per station (TOOLS/adjoint_source.py);
+  python -m ses3d_gb300 generate-models --root DIR [--profile TABLE] [--perturb [BLOCKDIR]]
+      writes MODELS/MODELS (boxfile, per-rank records) and DATA/COORDINATES for the tree's
+      INPUT/setup (generate_models.f90), optionally adding the block-model perturbations of
+      MODELS/MODELS_3D (add_perturbation.f90). TABLE: one layer per line, top depth [km],
+      rho [g/cm^3], vp, vs [km/s][, Q]; without it the homogeneous model (model_type 1).
 """
 import argparse
 import json
@@ -46,10 +51,17 @@ def main(argv=None):
     q.add_argument("--bandpass", type=float, nargs=2, default=None, metavar=("FMIN", "FMAX"))
     q.add_argument("--integrate", action="store_true", help="integrate velocity to displacement first")
     q.add_argument("--depth", type=float, default=None, help="adjoint source depth [m] (default: receiver's)")
+    gm = sub.add_parser("generate-models")
+    gm.add_argument("--root", required=True, help="SES3D tree holding INPUT/setup")
+    gm.add_argument("--profile", default=None, help="layered 1-D profile table")
+    gm.add_argument("--perturb", nargs="?", const="", default=None, help="add block perturbations")
+    gm.add_argument("--no-coordinates", action="store_true")
     a = ap.parse_args(argv)
 
     if a.cmd == "adjoint-sources":
         return adjoint_sources_cmd(a)
+    if a.cmd == "generate-models":
+        return generate_models_cmd(a)
 
     from . import synth
     if a.cmd == "generate":
@@ -107,6 +119,19 @@ def adjoint_sources_cmd(a):
         sources.append(src)
     AS.write_adjoint_directory(a.out, sources, depth=a.depth)
     print(json.dumps({"adjoint_sources": len(sources), "kind": a.kind, "out": a.out}))
+    return 0
+
+
+def generate_models_cmd(a):
+    import os
+    from . import formats as F
+    from . import models as M
+    setup = F.read_setup(os.path.join(a.root, "INPUT", "setup"))
+    prof = M.LayeredProfile.read(a.profile) if a.profile else None
+    boxes = M.generate_models(setup, a.root, prof, coordinates=not a.no_coordinates)
+    if a.perturb is not None:
+        M.add_perturbation_tree(a.root, a.perturb or None)
+    print(json.dumps({"boxes": len(boxes), "root": a.root, "perturbed": a.perturb is not None}))
     return 0
 
 
