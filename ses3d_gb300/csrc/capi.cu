@@ -534,6 +534,13 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   c.s_grad = (float)cfg->samp_ad * cfg->dt;
   c.pml = cfg->pml;
   c.lean = 0;
+  {  // magic multiplier for t / GX in k_node: l = ceil(log2 GX), m = floor(2^32 (2^l - GX) / GX) + 1
+    const unsigned long long d = (unsigned long long)g.GX;
+    int l = 0;
+    while ((1ull << l) < d) ++l;
+    c.gx_magic = (unsigned)((((1ull << 32) * ((1ull << l) - d)) / d + 1) & 0xffffffffull);
+    c.gx_shift = l - 1;
+  }
   c.Jac = g.Jac;
   c.inv_jac = 1.f / g.Jac;
   // coefficient tables

@@ -21,8 +21,8 @@
 #ifndef SES3D_NODE_MINB
 #define SES3D_NODE_MINB 6
 #endif
-#ifndef SES3D_NODE_TX
-#define SES3D_NODE_TX 0
+#ifndef SES3D_NODE_MAGIC
+#define SES3D_NODE_MAGIC 1
 #endif
 
 namespace ses3d {
@@ -611,21 +611,15 @@ __global__ void __launch_bounds__(256, SES3D_NODE_MINB) k_node(const Consts c, c
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
     *p.d_it += 1;  // every reader of the counter ran earlier in stream order
   const unsigned GXY = (unsigned)c.GX * (unsigned)c.GY;
-#if SES3D_NODE_TX
-  // CTA = NODE_TX x (256 / NODE_TX) tile of (gx, gy): the rows of one element's forces that
-  // neighbouring gy read come through the same L1
-  constexpr int TY = 256 / SES3D_NODE_TX;
-  const unsigned tiles_x = ((unsigned)c.GX + SES3D_NODE_TX - 1) / SES3D_NODE_TX;
-  const int gx = (int)((blockIdx.x % tiles_x) * SES3D_NODE_TX + threadIdx.x % SES3D_NODE_TX);
-  const int gy = (int)((blockIdx.x / tiles_x) * TY + threadIdx.x / SES3D_NODE_TX);
-  if (gx >= c.GX || gy >= c.GY) return;
-  const unsigned t = (unsigned)gx + (unsigned)c.GX * (unsigned)gy;
-#else
   const unsigned t = blockIdx.x * 256u + threadIdx.x;
   if (t >= GXY) return;
+#if SES3D_NODE_MAGIC
+  const unsigned hi = __umulhi(t, c.gx_magic);
+  const int gy = (int)((hi + ((t - hi) >> 1)) >> c.gx_shift);
+#else
   const int gy = (int)(t / (unsigned)c.GX);
-  const int gx = (int)t - gy * c.GX;
 #endif
+  const int gx = (int)t - gy * c.GX;
   const size_t g = (size_t)gz * GXY + t;
   // node-local loads first: they do not depend on the element forces
   float *V = p.v + (size_t)ev * 3 * c.G + g;
@@ -636,28 +630,51 @@ __global__ void __launch_bounds__(256, SES3D_NODE_MINB) k_node(const Consts c, c
   const int j0 = gy == 0 ? 0 : (gy - 1) >> 2, j1 = min(gy >> 2, c.ey - 1);
   const int k0 = gz == 0 ? 0 : (gz - 1) >> 2, k1 = min(gz >> 2, c.ez - 1);
   const float *F = p.f + (size_t)ev * 3 * (size_t)c.N;  // 3 N < 2^32 is checked at create
-  // all (up to 8) contributions are loaded first, then summed in the reference order;
-  // the offset of contribution (i, j, k) is the sum of one term per axis (see force_offset)
+  // Contributions (i, j, k) in {i0, i1} x {j0, j1} x {k0, k1}, summed in the reference
+  // order (i, then j, then k ascending). Whether a node lies on a y or z element face is
+  // the same for a warp of consecutive gx (one gy row), so the four cases below do not
+  // diverge; the x face (every fourth gx) is predicated. At most four contributions are
+  // in flight at a time.
   const unsigned sy_ = (unsigned)c.ex * 375u, sz_ = sy_ * (unsigned)c.ey;
-  const unsigned ox[2] = {(unsigned)i0 * 371u + (unsigned)gx, (unsigned)i1 * 371u + (unsigned)gx};  // 375 i + gx - 4 i
-  const unsigned oy[2] = {(unsigned)j0 * (sy_ - 20u) + 5u * (unsigned)gy, (unsigned)j1 * (sy_ - 20u) + 5u * (unsigned)gy};
-  const unsigned oz[2] = {(unsigned)k0 * (sz_ - 100u) + 25u * (unsigned)gz, (unsigned)k1 * (sz_ - 100u) + 25u * (unsigned)gz};
+  const unsigned q0 = ((unsigned)i0 * 371u + (unsigned)gx) + ((unsigned)j0 * (sy_ - 20u) + 5u * (unsigned)gy) +
+                      ((unsigned)k0 * (sz_ - 100u) + 25u * (unsigned)gz);
+  const unsigned dx = (unsigned)(i1 - i0) * 371u, dy = (unsigned)(j1 - j0) * (sy_ - 20u),
+                 dz = (unsigned)(k1 - k0) * (sz_ - 100u);
   const bool ux = i1 != i0, uy = j1 != j0, uz = k1 != k0;
-  float fx[8], fy[8], fz[8];
-#pragma unroll
-  for (int a = 0; a < 8; ++a) {
-    const bool use = (!(a & 4) || ux) && (!(a & 2) || uy) && (!(a & 1) || uz);
-    fx[a] = fy[a] = fz[a] = 0.f;
-    if (use) {
-      const unsigned q = ox[(a >> 2) & 1] + oy[(a >> 1) & 1] + oz[a & 1];
-      fx[a] = F[q]; fy[a] = F[q + 125]; fz[a] = F[q + 250];
-    }
-  }
   float sx = 0.f, sy = 0.f, sz = 0.f;
+  if (!uy && !uz) {
+    const float a0 = F[q0], a1 = F[q0 + 125], a2 = F[q0 + 250];
+    float b0 = 0.f, b1 = 0.f, b2 = 0.f;
+    if (ux) { b0 = F[q0 + dx]; b1 = F[q0 + dx + 125]; b2 = F[q0 + dx + 250]; }
+    sx = 0.f + a0; sy = 0.f + a1; sz = 0.f + a2;
+    if (ux) { sx += b0; sy += b1; sz += b2; }
+  } else if (!uy || !uz) {  // one of the y / z faces: contributions q0, q0 + d (+ the x pair)
+    const unsigned d = uz ? dz : dy;
+    const float a0 = F[q0], a1 = F[q0 + 125], a2 = F[q0 + 250];
+    const float c0 = F[q0 + d], c1 = F[q0 + d + 125], c2 = F[q0 + d + 250];
+    float b0 = 0.f, b1 = 0.f, b2 = 0.f, e0 = 0.f, e1 = 0.f, e2 = 0.f;
+    if (ux) {
+      b0 = F[q0 + dx]; b1 = F[q0 + dx + 125]; b2 = F[q0 + dx + 250];
+      e0 = F[q0 + dx + d]; e1 = F[q0 + dx + d + 125]; e2 = F[q0 + dx + d + 250];
+    }
+    sx = 0.f + a0; sy = 0.f + a1; sz = 0.f + a2;
+    sx += c0; sy += c1; sz += c2;
+    if (ux) { sx += b0; sy += b1; sz += b2; sx += e0; sy += e1; sz += e2; }
+  } else {  // y and z faces: i0 half (4 contributions), then the i1 half
 #pragma unroll
-  for (int a = 0; a < 8; ++a) {
-    const bool use = (!(a & 4) || ux) && (!(a & 2) || uy) && (!(a & 1) || uz);
-    if (use) { sx += fx[a]; sy += fy[a]; sz += fz[a]; }
+    for (int h = 0; h < 2; ++h) {
+      if (h == 1 && !ux) break;
+      const unsigned q = q0 + (h ? dx : 0u);
+      const float f00 = F[q], f01 = F[q + 125], f02 = F[q + 250];
+      const float f10 = F[q + dz], f11 = F[q + dz + 125], f12 = F[q + dz + 250];
+      const float f20 = F[q + dy], f21 = F[q + dy + 125], f22 = F[q + dy + 250];
+      const float f30 = F[q + dy + dz], f31 = F[q + dy + dz + 125], f32 = F[q + dy + dz + 250];
+      if (h == 0) { sx = 0.f + f00; sy = 0.f + f01; sz = 0.f + f02; }
+      else { sx += f00; sy += f01; sz += f02; }
+      sx += f10; sy += f11; sz += f12;
+      sx += f20; sy += f21; sz += f22;
+      sx += f30; sy += f31; sz += f32;
+    }
   }
   // a = s / MM with the reciprocal of the mass matrix (ses3d_evolution.f90:318-320)
   const float ax = sx * imm, ay = sy * imm, az = sz * imm;
@@ -989,13 +1006,7 @@ cudaError_t launch_element(int diss, int mode, int epb, const Consts &c, const P
 }
 
 cudaError_t launch_node(const Consts &c, const Ptrs &p, cudaStream_t st) {
-#if SES3D_NODE_TX
-  constexpr int TY = 256 / SES3D_NODE_TX;
-  dim3 grid((unsigned)((c.GX + SES3D_NODE_TX - 1) / SES3D_NODE_TX) * (unsigned)((c.GY + TY - 1) / TY), (unsigned)c.GZ,
-            (unsigned)c.nev);
-#else
   dim3 grid((unsigned)(((long long)c.GX * c.GY + 255) / 256), (unsigned)c.GZ, (unsigned)c.nev);
-#endif
   k_node<<<grid, 256, 0, st>>>(c, p);
   return cudaGetLastError();
 }

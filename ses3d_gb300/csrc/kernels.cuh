@@ -53,6 +53,10 @@ struct Consts {
   float tau_p[3], D_p[3];
   int pml;        // PML width in elements
   int lean;       // plain forward: displacement gradients kept only in PML elements
+  // t / GX for 32-bit t as (m + ((t - m) >> 1)) >> shift with m = umulhi(t, gx_magic)
+  // (division by an invariant integer, Granlund & Montgomery 1994); GX >= 2
+  unsigned gx_magic;
+  int gx_shift;
 };
 
 struct Ptrs {
