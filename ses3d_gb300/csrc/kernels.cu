@@ -830,25 +830,43 @@ __global__ void k_derive(const float *__restrict__ raw, float *__restrict__ mat,
   }
 }
 
-// Material coefficients from the reference layout (NMAT x N, element index fastest) into
-// element blocks [E][NMAT][128] (nodes 125..127 zero).
-__global__ void k_pack_mat(const float *__restrict__ ref, float *__restrict__ out, long long E) {
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= E * ELEM_MAT) return;
-  const long long e = q / ELEM_MAT;
-  const int r = (int)(q - e * ELEM_MAT), f = r / MAT_ROW, n = r % MAT_ROW;
-  out[q] = n < 125 ? ref[(long long)f * E * 125 + (long long)n * E + e] : 0.f;
-}
-
-// One state field of one event between the element-blocked state and the reference layout.
-__global__ void k_state_field(float *__restrict__ state_ev, int field, float *__restrict__ ref, long long E, int to_ref) {
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // reference index
-  if (q >= E * 125) return;
-  const long long e = q % E;
-  const int n = (int)(q / E);
-  float *sp = state_ev + (e * NSTATE + field) * 125 + n;
-  if (to_ref) ref[q] = *sp;
-  else *sp = ref[q];
+// Element-blocked fields <-> the reference layout, as a 32 x 32 shared-memory transpose:
+// blocked[e * stride + off + n] (n < 125; n < 128 with zero padding) <-> ref[n * E + e].
+// grid (ceil(E / 32), 4, nfields); field z uses off + z * field_step and ref + z * 125 E.
+__global__ void k_blocked_ref(float *__restrict__ blocked, long long stride, long long off, long long field_step,
+                              float *__restrict__ ref, long long E, int to_ref, int pad) {
+  __shared__ float tile[32][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const long long e0 = (long long)blockIdx.x * 32;
+  const int n0 = blockIdx.y * 32;
+  float *blk = blocked + off + (long long)blockIdx.z * field_step;
+  float *rf = ref + (long long)blockIdx.z * 125 * E;
+  const int nmax = pad ? 128 : 125;
+  if (!to_ref) {
+    for (int r = ty; r < 32; r += 8) {
+      const int n = n0 + r;
+      const long long e = e0 + tx;
+      tile[r][tx] = (n < 125 && e < E) ? rf[(long long)n * E + e] : 0.f;
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+      const long long e = e0 + r;
+      const int n = n0 + tx;
+      if (e < E && n < nmax) blk[e * stride + n] = tile[tx][r];
+    }
+  } else {
+    for (int r = ty; r < 32; r += 8) {
+      const long long e = e0 + r;
+      const int n = n0 + tx;
+      if (e < E && n < 125) tile[tx][r] = blk[e * stride + n];
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+      const int n = n0 + r;
+      const long long e = e0 + tx;
+      if (n < 125 && e < E) rf[(long long)n * E + e] = tile[r][tx];
+    }
+  }
 }
 
 // Mirror stresses of the elements outside the PML from their partners (syx = sxy,
@@ -1065,14 +1083,15 @@ cudaError_t launch_mass(const Consts &c, const float *rhoinv, const float *z, co
 }
 
 cudaError_t launch_pack_mat(const float *ref, float *out, long long E, cudaStream_t st) {
-  const long long n = E * ELEM_MAT;
-  k_pack_mat<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ref, out, E);
+  // material: [e][NMAT][128], nodes 125..127 zero
+  k_blocked_ref<<<dim3((unsigned)((E + 31) / 32), 4, NMAT), dim3(32, 8), 0, st>>>(
+      out, ELEM_MAT, 0, MAT_ROW, const_cast<float *>(ref), E, 0, 1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_state_field(float *state_ev, int field, float *ref, long long E, int to_ref, cudaStream_t st) {
-  const long long n = E * 125;
-  k_state_field<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(state_ev, field, ref, E, to_ref);
+  k_blocked_ref<<<dim3((unsigned)((E + 31) / 32), 4, 1), dim3(32, 8), 0, st>>>(
+      state_ev, ELEM_STATE, (long long)field * 125, 0, ref, E, to_ref, 0);
   return cudaGetLastError();
 }
 
