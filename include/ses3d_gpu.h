@@ -211,6 +211,13 @@ long ses3d_gpu_get_setup_real(ses3d_gpu *h, int event, const char *name, float *
  * reference prints every step, SOURCE/ses3d_main.f90:111-130). */
 int ses3d_gpu_vmax(ses3d_gpu *h, float *out);
 
+/* Self-test of the device-side failure path (no counterpart in the reference): launches a
+ * kernel whose wait on an mbarrier can never complete (it expects bytes no copy delivers)
+ * and that gives up after limit_ms, exactly as the element kernel's bounded waits do.
+ * Returns SES3D_E_CUDA with the bounded-wait message; the device error word is cleared
+ * and the handle stays usable. */
+int ses3d_gpu_selftest_wait(ses3d_gpu *h, int limit_ms);
+
 /* Device-resident interface (zero-copy for PyTorch / CUDA callers). Pointers are
  * device pointers on the handle's device; layouts are the reference layouts.
  * Model upload from device memory: */

@@ -30,6 +30,7 @@ cudaError_t launch_grad_q_norm(const Consts &c, const float *gm, double *grad, c
 cudaError_t launch_gather_ref(const Consts &c, const float *v, float *out, cudaStream_t st);
 cudaError_t prepare_element_kernels();
 cudaError_t launch_sync_mirrors(const Consts &c, float *state, cudaStream_t st);
+cudaError_t launch_wait_selftest(int *err, unsigned long long limit_ns, cudaStream_t st);
 cudaError_t launch_sum_events_d(const double *grad, int slot, int nev, long long N, double *out, cudaStream_t st);
 cudaError_t launch_pack_mat(const float *ref, float *out, long long E, cudaStream_t st);
 cudaError_t launch_state_field(float *state_ev, int field, float *ref, long long E, int to_ref, cudaStream_t st);
@@ -775,7 +776,7 @@ static int check_device_error(ses3d_gpu *h) {
   CK(h, cudaMemcpy(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err == 0) return SES3D_OK;
   CK(h, cudaMemset(h->d_err, 0, sizeof(int)));
-  return fail(h, SES3D_E_CUDA, "element kernel: a bulk copy into shared memory did not complete within 2 s");
+  return fail(h, SES3D_E_CUDA, "bounded wait expired: a bulk copy into shared memory did not complete in time");
 }
 
 int ses3d_gpu_step(ses3d_gpu *h, int n) {
@@ -1153,6 +1154,14 @@ long ses3d_gpu_get_setup_real(ses3d_gpu *h, int event, const char *name, float *
     return (long)g.N;
   }
   return fail(h, SES3D_E_CONFIG, "unknown setup real " + nm);
+}
+
+int ses3d_gpu_selftest_wait(ses3d_gpu *h, int limit_ms) {
+  if (!h) return SES3D_E_CONFIG;
+  if (limit_ms < 1 || limit_ms > 10000) return fail(h, SES3D_E_CONFIG, "limit_ms must be in 1..10000");
+  CK(h, launch_wait_selftest(h->d_err, (unsigned long long)limit_ms * 1000000ull, h->st));
+  CK(h, cudaStreamSynchronize(h->st));
+  return check_device_error(h);
 }
 
 int ses3d_gpu_vmax(ses3d_gpu *h, float *out) {

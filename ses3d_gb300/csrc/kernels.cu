@@ -19,7 +19,7 @@
 #endif
 // The same for k_node (256-thread CTAs).
 #ifndef SES3D_NODE_MINB
-#define SES3D_NODE_MINB 6
+#define SES3D_NODE_MINB 7
 #endif
 #ifndef SES3D_NODE_MAGIC
 #define SES3D_NODE_MAGIC 1
@@ -424,12 +424,13 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-// Waits for phase `parity` of bar; gives up after 2 s, recording the failure in *err.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity, int *err) {
+// Waits for phase `parity` of bar; gives up after limit_ns (2 s), recording the failure in *err.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity, int *err,
+                                                  unsigned long long limit_ns = 2000000000ull) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   while (!mbar_try_wait(bar, parity)) {
-    if (global_ns() - t0 > 2000000000ull) {
+    if (global_ns() - t0 > limit_ns) {
       atomicExch(err, 2);
       return false;
     }
@@ -1098,6 +1099,24 @@ cudaError_t launch_state_field(float *state_ev, int field, float *ref, long long
 cudaError_t launch_sync_mirrors(const Consts &c, float *state, cudaStream_t st) {
   const long long n = (long long)c.nev * c.E * 125;
   k_sync_mirrors<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(c, state);
+  return cudaGetLastError();
+}
+
+// Self-test of the bounded wait: one CTA arms an mbarrier for 16 bytes that no copy ever
+// delivers and waits on it with the element kernel's wait; the wait must give up after
+// limit_ns and leave its code in *err. No copy is in flight when the CTA exits.
+__global__ void k_wait_selftest(int *err, unsigned long long limit_ns) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_arrive_expect_tx(&bar, 16u);
+    mbar_wait_bounded(&bar, 0u, err, limit_ns);
+  }
+}
+
+cudaError_t launch_wait_selftest(int *err, unsigned long long limit_ns, cudaStream_t st) {
+  k_wait_selftest<<<1, 32, 0, st>>>(err, limit_ns);
   return cudaGetLastError();
 }
 

@@ -467,7 +467,11 @@ def read_records(path: str) -> List[np.ndarray]:
         data = f.read()
     pos = 0
     while pos < len(data):
+        if pos + 4 > len(data):
+            raise ValueError("truncated record in %s" % path)
         (n,) = struct.unpack_from("<i", data, pos)
+        if n < 0 or n % 4 or pos + 8 + n > len(data):
+            raise ValueError("truncated record in %s" % path)
         payload = data[pos + 4: pos + 4 + n]
         (m,) = struct.unpack_from("<i", data, pos + 4 + n)
         if m != n:
