@@ -8,9 +8,20 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/ses3d_gpu.h"
 #include "kernels.cuh"
 #include "setup.hpp"
+
+namespace {
+// NVTX range for the phases of a run (step, model set-up, checkpoint recompute, adjoint
+// start): visible in Nsight timelines, free when no tool is attached.
+struct Range {
+  explicit Range(const char *name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+};
+}  // namespace
 
 namespace ses3d {
 cudaError_t launch_element(int diss, int mode, int epb, const Consts &c, const Ptrs &p, cudaStream_t st);
@@ -405,6 +416,7 @@ size_t ckpt_floats(const ses3d_gpu *h) {
 }
 
 int save_checkpoint(ses3d_gpu *h, int completed_it) {
+  Range range_("ses3d checkpoint");
   const size_t ns = (size_t)h->cfg.n_events * NSTATE * h->geo.N;
   float *c = nullptr;
   CK(h, dalloc(&c, ckpt_floats(h)));
@@ -419,6 +431,7 @@ int save_checkpoint(ses3d_gpu *h, int completed_it) {
 // Recomputes the records of segment s (records s K .. min((s+1) K, nrec) - 1) into segbuf
 // by a forward run from checkpoint s on the second wavefield.
 int recompute_segment(ses3d_gpu *h, int s) {
+  Range range_("ses3d recompute segment");
   const size_t ns = (size_t)h->cfg.n_events * NSTATE * h->geo.N;
   const size_t nv = (size_t)h->cfg.n_events * 3 * h->geo.G;
   const size_t rec_floats = (size_t)h->cfg.n_events * NREC * h->geo.N;
@@ -456,6 +469,7 @@ int recompute_segment(ses3d_gpu *h, int s) {
 }
 
 int build_graph(ses3d_gpu *h) {
+  Range range_("ses3d graph capture");
   destroy_graph(h);
   cudaGraph_t graph;
   CK(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
@@ -650,6 +664,7 @@ int ses3d_gpu_destroy(ses3d_gpu *h) {
 
 int ses3d_gpu_set_model(ses3d_gpu *h, const float *rhoinv, const float *mu, const float *lambda, const float *A,
                         const float *B, const float *C, const float *Q) {
+  Range range_("ses3d set model");
   if (!h) return SES3D_E_CONFIG;
   if (!rhoinv || !mu || !lambda || !A || !B || !C) return fail(h, SES3D_E_CONFIG, "null model array");
   if (h->cfg.is_diss && !Q) return fail(h, SES3D_E_CONFIG, "Q is required when is_diss = 1");
@@ -780,6 +795,7 @@ static int check_device_error(ses3d_gpu *h) {
 }
 
 int ses3d_gpu_step(ses3d_gpu *h, int n) {
+  Range range_("ses3d step");
   if (!h) return SES3D_E_CONFIG;
   if (!h->model_set) return fail(h, SES3D_E_STATE, "set_model must be called before step");
   if (n < 0) return fail(h, SES3D_E_CONFIG, "n must be >= 0");
@@ -1048,6 +1064,7 @@ int ses3d_gpu_set_saving_vector(ses3d_gpu *h, const int *in) {
 }
 
 int ses3d_gpu_begin_adjoint(ses3d_gpu *h) {
+  Range range_("ses3d begin adjoint");
   if (!h) return SES3D_E_CONFIG;
   h->mode_flag = 2;
   h->cfg.adjoint_flag = 2;

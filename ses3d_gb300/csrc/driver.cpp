@@ -15,6 +15,7 @@
 //   ses3d_gpu_main [--main DIR] [--pml N] [--grad-q] [--max-elements NX NY NZ]
 //                  [--stitch-model OUTDIR]
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -139,6 +140,7 @@ int stitch_model(const Args &a) {
 }
 
 int run_event(const Args &a, const std::string &id) {
+  const auto t_start = std::chrono::steady_clock::now();
   std::string err;
   const std::string in = join(a.main, "../INPUT/");
   // ---- ses3d_input (SOURCE/ses3d_input.f90:44-618)
@@ -310,8 +312,12 @@ int run_event(const Args &a, const std::string &id) {
         if (!write_split(dec, ffd + kRecordNames[f] + "_", "", &one[(size_t)f * N], r > 0, err)) return die(err);
     }
   }
-  std::printf("event %s: %d iterations, %d receivers, %lld launches\n", id.c_str(), cfg.nt, nr,
-              (long long)ses3d_gpu_launch_count(h));
+  // one structured line per event (the reference logs a line per step instead)
+  const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  std::printf("{\"event\": \"%s\", \"iterations\": %d, \"receivers\": %d, \"boxes\": %zu, \"gll_points\": %zu, "
+              "\"launches\": %lld, \"seconds\": %.6f, \"gll_point_steps_per_s\": %.6e}\n",
+              id.c_str(), cfg.nt, nr, dec.boxes.size(), N, (long long)ses3d_gpu_launch_count(h), secs,
+              secs > 0 ? (double)N * cfg.nt / secs : 0.0);
   ses3d_gpu_destroy(h);
   return 0;
 }

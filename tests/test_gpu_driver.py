@@ -1,6 +1,7 @@
 """ses3d_gpu_main, the reference program flow on the GPU library: run on generated SES3D
 directory trees, its output files (seismograms, snapshots, forward-field records,
 saving_vector, grad_* kernels) are compared with the oracle."""
+import json
 import os
 import subprocess
 
@@ -36,7 +37,8 @@ def test_forward_tree(native, oracle_mod, tmp_path):
     root = str(tmp_path)
     synth.write_problem(p, root)
     out = run_driver(root, p.pml)
-    assert "40 iterations" in out
+    summary = json.loads(out.strip().splitlines()[-1])
+    assert summary["iterations"] == 40 and summary["boxes"] == 1 and summary["gll_points"] == p.n_nodes
     ofd = os.path.join(root, "MAIN", "../DATA/OUTPUT/1/")
     o = oracle_mod.Oracle(p)
     o.run(20)
