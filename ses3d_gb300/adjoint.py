@@ -81,6 +81,20 @@ class EventData:
 
 
 @dataclass
+class MemoryPlan:
+    """Sub-batches of `events_per_batch` events, checkpoint segment length K (0: keep
+    every record)."""
+    events_per_batch: int
+    K: int
+    n_events: int
+
+    @property
+    def groups(self) -> List[List[int]]:
+        g = self.events_per_batch
+        return [list(range(a, min(a + g, self.n_events))) for a in range(0, self.n_events, g)]
+
+
+@dataclass
 class MisfitSetup:
     """Mesh, time axis and events of a misfit; built from a synth.Problem by from_problem."""
     cfg_template: object
@@ -88,7 +102,7 @@ class MisfitSetup:
     fmin: float = 1.0 / 50.0
     fmax: float = 1.0 / 10.0
     samp_ad: int = 10
-    memory_budget: Optional[float] = None  # bytes for records of all events; None: free device memory
+    memory_budget: Optional[float] = None  # device bytes a gradient may use; None: free device memory
     grad_q: bool = True
     last: dict = field(default_factory=dict)
 
@@ -105,70 +119,103 @@ class MisfitSetup:
         return cls(cfg, evs, samp_ad=samp_ad, **kw)
 
     # -- simulation plumbing --------------------------------------------------------------------
-    def _config(self, adjoint_flag: int):
+    def _config(self, adjoint_flag: int, n_events: Optional[int] = None):
         c = L.Config()
         ctypes_copy(c, self.cfg_template)
         c.adjoint_flag = adjoint_flag
         c.samp_ad = self.samp_ad
-        c.n_events = len(self.events)
+        c.n_events = len(self.events) if n_events is None else n_events
         c.grad_variant = 1 if self.grad_q else 0
         return c
 
-    def simulate(self, records: dict, adjoint: bool = False) -> Simulation:
-        """Forward run of all events on the given model records (device tensors)."""
-        sim = Simulation(self._config(1 if adjoint else 0))
+    def simulate(self, records: dict, adjoint: bool = False, events: Optional[Sequence[int]] = None,
+                 K: Optional[int] = None) -> Simulation:
+        """Forward run of the given events (default: all) on the model records (device
+        tensors). adjoint: keep the forward records, or checkpoints every K records."""
+        evs = list(range(len(self.events))) if events is None else list(events)
+        sim = Simulation(self._config(1 if adjoint else 0, len(evs)))
         sim.set_model_device([records[k].data_ptr() if k in records else 0 for k in
                               ("rhoinv", "mu", "lambda", "A", "B", "C", "Q")])
-        for k, e in enumerate(self.events):
-            sim.set_source(k, e.xxs, e.yys, e.zzs, e.source_type, e.mom, e.stf)
-            sim.set_receivers(k, e.recloc)
+        for slot, k in enumerate(evs):
+            e = self.events[k]
+            sim.set_source(slot, e.xxs, e.yys, e.zzs, e.source_type, e.mom, e.stf)
+            sim.set_receivers(slot, e.recloc)
         if adjoint:
-            K = self.segment_length(sim)
+            if K is None:
+                K = self.plan().K
             if K:
                 L.check(sim.lib.ses3d_gpu_set_checkpointing(sim.h, K), sim.h)
             self.last["records_per_segment"] = K
         sim.run()
         return sim
 
-    def record_budget(self, sim: Simulation) -> float:
-        """Bytes available for forward records: memory_budget, or else the free device
-        memory less what the adjoint run allocates later (FP64 kernel accumulators, 64 B
-        per GLL point and event) and a reserve (5 % of the device, at least 8 GB)."""
+    # -- memory plan ---------------------------------------------------------------------------
+    def budget(self) -> float:
+        """Device bytes a gradient may use: memory_budget, or the free device memory less a
+        reserve (5 % of the device, at least 8 GB)."""
         if self.memory_budget is not None:
             return float(self.memory_budget)
         import torch
         free, total = torch.cuda.mem_get_info()
-        grad_b = 64.0 * sim.N * sim.n_events
-        return max(0.0, float(free) - grad_b - max(8e9, 0.05 * float(total)))
+        return max(0.0, float(free) - max(8e9, 0.05 * float(total)))
 
-    def segment_length(self, sim: Simulation) -> int:
-        """0 (keep every record) if all records fit the budget, else the checkpoint segment
-        length K that minimises checkpoint + segment memory."""
-        nt, s = sim.nt, self.samp_ad
-        nrec = len([it for it in range(1, nt + 1) if it % s == 0 or it == 1 or it == nt])
-        rec_b = 9.0 * sim.N * 4 * sim.n_events
-        ck_b = (36.0 * sim.N + 3.0 * sim.G) * 4 * sim.n_events
-        if nrec * rec_b <= self.record_budget(sim):
-            return 0
-        K = max(1, int(round(math.sqrt(nrec * ck_b / rec_b))))
-        return K
+    def plan(self) -> "MemoryPlan":
+        """Events per sub-batch and checkpoint segment length K (0: every record kept) so
+        that one sub-batch's device memory fits the budget. Per event: element state,
+        velocity and forces, FP64 kernel accumulators, and either every record (9 floats
+        per GLL point and stored iteration) or ceil(nrec / K) full-state checkpoints, K
+        records and a second wavefield; shared per handle: material, geometry, mass
+        matrix. The largest sub-batch that fits wins; K minimises checkpoint + segment
+        memory. With nothing fitting, one event per sub-batch with checkpoints."""
+        shared, keep, with_ckpt, K = self.memory_model()
+        budget = self.budget()
+        nev = len(self.events)
+        for g in range(nev, 0, -1):
+            if shared + g * keep <= budget:
+                return MemoryPlan(g, 0, nev)
+            if shared + g * with_ckpt <= budget:
+                return MemoryPlan(g, K, nev)
+        return MemoryPlan(1, K, nev)
+
+    def memory_model(self):
+        """(bytes per handle, per event keeping every record, per event with checkpoints
+        every K records, K)."""
+        c = self.cfg_template
+        E = (c.nx + 1) * (c.ny + 1) * (c.nz + 1)
+        N, G = 125.0 * E, float((4 * c.nx + 5) * (4 * c.ny + 5) * (4 * c.nz + 5))
+        nt, smp = int(c.nt), self.samp_ad
+        nrec = len([it for it in range(1, nt + 1) if it % smp == 0 or it == 1 or it == nt])
+        shared = 64.0 * N + 12.0 * G
+        event = (36.0 * N + 3.0 * G + 3.0 * N) * 4 + 64.0 * N
+        rec = 36.0 * N
+        ckpt = (36.0 * N + 3.0 * G) * 4
+        K = max(1, int(round(math.sqrt(nrec * ckpt / rec))))
+        return shared, event + nrec * rec, event + ckpt + math.ceil(nrec / K) * ckpt + K * rec, K
 
     def filt(self, nt: int, dt: float) -> Bandpass:
         return Bandpass(nt, dt, self.fmin, self.fmax)
 
     def seismograms(self, sim: Simulation) -> List[np.ndarray]:
+        """(3, nr, nt) FP64 per event of the handle (its events in slot order)."""
         out = []
-        for k in range(len(self.events)):
+        for k in range(sim.n_events):
             sx, sy, sz = sim.seismograms(k)
             out.append(np.stack([sx, sy, sz]).astype(np.float64))  # (3, nr, nt)
         return out
 
+    def forward_seismograms(self, records: dict) -> List[np.ndarray]:
+        """Plain forward seismograms of every event, sub-batched like the gradient."""
+        syn = []
+        for grp in self.plan().groups:
+            sim = self.simulate(records, events=grp)
+            syn += self.seismograms(sim)
+            sim.close()
+        return syn
+
     def set_observed(self, model_tensors: Sequence):
         """Observed data = synthetics of the given (rho, vp, vsh, vsv, Q) model."""
-        sim = self.simulate(model_records(*model_tensors))
-        for e, s in zip(self.events, self.seismograms(sim)):
+        for e, s in zip(self.events, self.forward_seismograms(model_records(*model_tensors))):
             e.observed = s
-        sim.close()
 
     def misfit_value(self, syn: List[np.ndarray], dt: float) -> float:
         F = self.filt(syn[0].shape[-1], dt)
@@ -236,11 +283,17 @@ class _Misfit:
             @staticmethod
             def forward(ctx, setup: MisfitSetup, rho, vp, vsh, vsv, Q):
                 recs = model_records(rho, vp, vsh, vsv, Q)
-                sim = setup.simulate(recs, adjoint=True)
-                dt = float(sim.cfg.dt)
-                syn = setup.seismograms(sim)
+                plan = setup.plan()
+                setup.last["plan"] = plan
+                if len(plan.groups) == 1:  # one handle keeps the forward records for backward
+                    sim = setup.simulate(recs, adjoint=True, K=plan.K)
+                    syn = setup.seismograms(sim)
+                    ctx.sim = sim
+                else:                      # sub-batches: plain forward now, recomputed in backward
+                    syn, ctx.sim = setup.forward_seismograms(recs), None
+                dt = float(setup.cfg_template.dt)
                 chi = setup.misfit_value(syn, dt)
-                ctx.setup, ctx.sim, ctx.syn, ctx.dt = setup, sim, syn, dt
+                ctx.setup, ctx.syn, ctx.dt, ctx.recs, ctx.plan = setup, syn, dt, recs, plan
                 ctx.save_for_backward(Q)
                 setup.last["seismograms"] = syn
                 return torch.tensor(chi, dtype=torch.float64, device=rho.device)
@@ -248,23 +301,32 @@ class _Misfit:
             @staticmethod
             def backward(ctx, grad_out):
                 (Q,) = ctx.saved_tensors
-                setup, sim, syn, dt = ctx.setup, ctx.sim, ctx.syn, ctx.dt
+                setup, syn, dt, plan = ctx.setup, ctx.syn, ctx.dt, ctx.plan
                 srcs = setup.adjoint_sources(syn, dt, setup.last.get("shift", 0.0))
-                for k, e in enumerate(setup.events):
-                    sim.set_adjoint_sources(k, e.recloc, srcs[k])
-                sim.begin_adjoint()
-                sim.run()
-                W, jac = quadrature_volume(sim)
+                names = ("rho", "cp", "csh", "csv", "Q_mu")
+                ksum = None
+                W = jac = None
+                for grp in plan.groups:
+                    sim = ctx.sim if ctx.sim is not None else setup.simulate(ctx.recs, adjoint=True, events=grp,
+                                                                             K=plan.K)
+                    for slot, k in enumerate(grp):
+                        sim.set_adjoint_sources(slot, setup.events[k].recloc, srcs[k])
+                    sim.begin_adjoint()
+                    sim.run()
+                    if W is None:
+                        W, jac = quadrature_volume(sim)
+                    # events added in index order: within a sub-batch on the device, then
+                    # sub-batch by sub-batch
+                    part = [sim.kernel_sum(nm) for nm in names]
+                    ksum = part if ksum is None else [a + b for a, b in zip(ksum, part)]
+                    sim.close()
+                ctx.sim = None
                 # ses3d's kernel sign convention: dchi = -Jac sum W K dm (checked against FD)
                 scale = -float(grad_out) * jac
                 dev = Q.device
-                grads = []
-                for name in ("rho", "cp", "csh", "csv", "Q_mu"):
-                    g = sim.kernel_sum(name) * W * scale
-                    grads.append(torch.from_numpy(g).to(dev))
+                grads = [torch.from_numpy(k * W * scale).to(dev) for k in ksum]
                 grads[4] = grads[4] / Q.double()
                 setup.last["kernels"] = {n: g for n, g in zip(("rho", "vp", "vsh", "vsv", "Q"), grads)}
-                sim.close()
                 return (None,) + tuple(g.to(Q.dtype) for g in grads)
 
         return WaveformMisfit
@@ -283,10 +345,8 @@ def waveform_misfit(setup: MisfitSetup, rho, vp, vsh, vsv, Q):
 
 def misfit_only(setup: MisfitSetup, rho, vp, vsh, vsv, Q) -> float:
     """chi without keeping records (finite-difference checks)."""
-    sim = setup.simulate(model_records(rho, vp, vsh, vsv, Q))
-    chi = setup.misfit_value(setup.seismograms(sim), float(sim.cfg.dt))
-    sim.close()
-    return chi
+    syn = setup.forward_seismograms(model_records(rho, vp, vsh, vsv, Q))
+    return setup.misfit_value(syn, float(setup.cfg_template.dt))
 
 
 def problem_tensors(p, device="cuda"):

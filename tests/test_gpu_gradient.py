@@ -82,3 +82,37 @@ def test_checkpointed_gradient_equals_stored(native):
         assert (setup.last["records_per_segment"] > 0) == (budget < 10)
     for a, b in zip(*grads):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("per_batch,ckpt", [(1, False), (2, True)])
+def test_sub_batched_gradient_equals_one_batch(native, per_batch, ckpt):
+    """A budget that admits only per_batch events at a time runs the events in sub-batches
+    (forward recomputed in the backward pass) and gives the one-batch gradient."""
+    import torch
+    from ses3d_gb300 import adjoint as A
+    # checkpoints pay off only beyond ~40 records: 300 steps store 61
+    p = synth.make_problem("tiny", nt=300 if ckpt else 80, seed=47, adjoint_flag=1, n_events=3)
+    for k, e in enumerate(p.events):
+        e.event.zzs = np.float32(6000.0 + 7000.0 * k)
+    grads, plans = [], []
+    for sub in (False, True):
+        setup = A.MisfitSetup.from_problem(p, samp_ad=5, fmin=1 / 40, fmax=1 / 8)
+        shared, keep, with_ckpt, K = setup.memory_model()
+        per = with_ckpt if ckpt else keep
+        setup.memory_budget = (shared + per * (per_batch + 0.5)) if sub else 1e13
+        if sub and ckpt:
+            assert shared + keep * per_batch > setup.memory_budget      # records alone do not fit
+        setup.set_observed([t * 1.01 for t in A.problem_tensors(p)])
+        ms = [t.clone().requires_grad_(True) for t in A.problem_tensors(p)]
+        chi = A.waveform_misfit(setup, *ms)
+        chi.backward()
+        grads.append((float(chi.detach()), [m.grad.cpu().numpy() for m in ms]))
+        plans.append(setup.last["plan"])
+    assert len(plans[0].groups) == 1 and plans[1].events_per_batch == per_batch
+    assert (plans[1].K > 0) == ckpt
+    assert grads[0][0] == grads[1][0]
+    for a, b in zip(grads[0][1], grads[1][1]):
+        if per_batch == 1:
+            assert np.array_equal(a, b)              # same FP64 summation order
+        else:
+            assert np.allclose(a, b, rtol=1e-12, atol=0)
