@@ -225,14 +225,17 @@ class MisfitSetup:
             chi += 0.5 * float(np.sum(r * r)) * dt
         return chi
 
-    def adjoint_sources(self, syn: List[np.ndarray], dt: float, shift: float = 0.0):
-        """Per event: (nr, 3, nt) forces in adjoint-iteration order. The force density is the
-        functional derivative of chi = 1/2 int |F(u - d)|^2 dt, i.e. F^T F (u - d)(t) per unit
-        time; `shift` delays it by a fraction of a sample (alignment studies)."""
+    def adjoint_sources(self, syn: List[np.ndarray], dt: float, shift: float = 0.0,
+                        events: Optional[Sequence[int]] = None):
+        """Per event (all, or the listed ones, matching syn): (nr, 3, nt) forces in
+        adjoint-iteration order. The force density is the functional derivative of
+        chi = 1/2 int |F(u - d)|^2 dt, i.e. F^T F (u - d)(t) per unit time; `shift` delays
+        it by a fraction of a sample (alignment studies)."""
         nt = syn[0].shape[-1]
         F = self.filt(nt, dt)
         out = []
-        for e, s in zip(self.events, syn):
+        evs = self.events if events is None else [self.events[k] for k in events]
+        for e, s in zip(evs, syn):
             a = F(F(s - e.observed))                        # dchi/du_vel(t), (3, nr, nt)
             if shift:
                 fr = np.fft.rfftfreq(F.nfft, dt)
@@ -272,6 +275,9 @@ def quadrature_volume(sim: Simulation):
     return out.reshape(-1), jac
 
 
+KERNEL_NAMES = ("rho", "cp", "csh", "csv", "Q_mu")
+
+
 class _Misfit:
     """torch.autograd.Function factory (keeps torch an optional import)."""
 
@@ -285,42 +291,54 @@ class _Misfit:
                 recs = model_records(rho, vp, vsh, vsv, Q)
                 plan = setup.plan()
                 setup.last["plan"] = plan
+                dt = float(setup.cfg_template.dt)
+                ctx.setup, ctx.dt, ctx.plan = setup, dt, plan
+                ctx.save_for_backward(Q)
                 if len(plan.groups) == 1:  # one handle keeps the forward records for backward
                     sim = setup.simulate(recs, adjoint=True, K=plan.K)
                     syn = setup.seismograms(sim)
-                    ctx.sim = sim
-                else:                      # sub-batches: plain forward now, recomputed in backward
-                    syn, ctx.sim = setup.forward_seismograms(recs), None
-                dt = float(setup.cfg_template.dt)
+                    ctx.sim, ctx.syn, ctx.kernels = sim, syn, None
+                else:
+                    # sub-batches: an event's adjoint sources depend on its own residual only,
+                    # so each sub-batch runs forward, adjoint and kernel sum here and is freed;
+                    # backward scales the summed kernels
+                    syn, ksum, W, jac = [], None, None, None
+                    for grp in plan.groups:
+                        sim = setup.simulate(recs, adjoint=True, events=grp, K=plan.K)
+                        sg = setup.seismograms(sim)
+                        srcs = setup.adjoint_sources(sg, dt, setup.last.get("shift", 0.0), events=grp)
+                        for slot, k in enumerate(grp):
+                            sim.set_adjoint_sources(slot, setup.events[k].recloc, srcs[slot])
+                        sim.begin_adjoint()
+                        sim.run()
+                        if W is None:
+                            W, jac = quadrature_volume(sim)
+                        part = [sim.kernel_sum(nm) for nm in KERNEL_NAMES]   # events in index order
+                        ksum = part if ksum is None else [a + b for a, b in zip(ksum, part)]
+                        sim.close()
+                        syn += sg
+                    ctx.sim, ctx.syn, ctx.kernels = None, syn, (ksum, W, jac)
                 chi = setup.misfit_value(syn, dt)
-                ctx.setup, ctx.syn, ctx.dt, ctx.recs, ctx.plan = setup, syn, dt, recs, plan
-                ctx.save_for_backward(Q)
                 setup.last["seismograms"] = syn
                 return torch.tensor(chi, dtype=torch.float64, device=rho.device)
 
             @staticmethod
             def backward(ctx, grad_out):
                 (Q,) = ctx.saved_tensors
-                setup, syn, dt, plan = ctx.setup, ctx.syn, ctx.dt, ctx.plan
-                srcs = setup.adjoint_sources(syn, dt, setup.last.get("shift", 0.0))
-                names = ("rho", "cp", "csh", "csv", "Q_mu")
-                ksum = None
-                W = jac = None
-                for grp in plan.groups:
-                    sim = ctx.sim if ctx.sim is not None else setup.simulate(ctx.recs, adjoint=True, events=grp,
-                                                                             K=plan.K)
-                    for slot, k in enumerate(grp):
-                        sim.set_adjoint_sources(slot, setup.events[k].recloc, srcs[k])
+                setup, syn, dt = ctx.setup, ctx.syn, ctx.dt
+                if ctx.kernels is None:
+                    sim = ctx.sim
+                    srcs = setup.adjoint_sources(syn, dt, setup.last.get("shift", 0.0))
+                    for k, e in enumerate(setup.events):
+                        sim.set_adjoint_sources(k, e.recloc, srcs[k])
                     sim.begin_adjoint()
                     sim.run()
-                    if W is None:
-                        W, jac = quadrature_volume(sim)
-                    # events added in index order: within a sub-batch on the device, then
-                    # sub-batch by sub-batch
-                    part = [sim.kernel_sum(nm) for nm in names]
-                    ksum = part if ksum is None else [a + b for a, b in zip(ksum, part)]
+                    W, jac = quadrature_volume(sim)
+                    ksum = [sim.kernel_sum(nm) for nm in KERNEL_NAMES]
                     sim.close()
-                ctx.sim = None
+                    ctx.sim = None
+                else:
+                    ksum, W, jac = ctx.kernels
                 # ses3d's kernel sign convention: dchi = -Jac sum W K dm (checked against FD)
                 scale = -float(grad_out) * jac
                 dev = Q.device
