@@ -74,3 +74,22 @@ def test_driver_builds_and_reports_missing_gpu(native, tmp_path):
     synth.write_problem(p, str(tmp_path))
     res = subprocess.run([drv, "--main", str(tmp_path / "MAIN"), "--pml", "3"], capture_output=True, text=True)
     assert res.returncode == 1 and "no CUDA device" in res.stderr
+
+
+def test_fortran_interface_block_covers_header():
+    """INTEGRATION.md's ISO_C_BINDING module declares every entry point of the header,
+    with the header's return kind."""
+    import re
+    h = open(os.path.join(ROOT, "include", "ses3d_gpu.h")).read()
+    decl = dict((name, ret) for ret, name in re.findall(r"^(const char \*|void \*|int64_t|long|int) ?(ses3d_gpu_\w+)\(",
+                                                        h, re.M))
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    a = doc.index("```fortran")
+    block = doc[a:doc.index("```", a + 10)]
+    fort = dict((name, kind) for kind, name in re.findall(r"(integer\(c_\w+\)|type\(c_ptr\)) function (ses3d_gpu_\w+)",
+                                                          block))
+    assert set(decl) == set(fort), sorted(set(decl) ^ set(fort))
+    want = {"int": "integer(c_int)", "long": "integer(c_long)", "int64_t": "integer(c_int64_t)",
+            "const char *": "type(c_ptr)", "void *": "type(c_ptr)"}
+    for name, ret in decl.items():
+        assert fort[name] == want[ret], (name, ret, fort[name])
