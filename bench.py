@@ -262,6 +262,8 @@ def run_ours(args, rank, world, local):
         cfg_sim = Simulation.from_problem(p, nt=args.steps, model=False)
         cfg_sim.set_lean(args.lean)
         cfg_sim.set_model(pinned)
+        if args.graph:
+            cfg_sim.use_graph(True, args.graph)
         cfg_sim.step(args.steps)
         out = cfg_sim.seismograms(0)
         t1 = time.perf_counter()

@@ -194,17 +194,24 @@ std::vector<Receiver> locate_receivers(const Geometry &g, int nr_global, const f
       continue;
     Receiver r;  // a receiver in the box that matches no element keeps zeros, as the reference's static arrays
     r.global_index = n;
+    // The reference tests every element (i outer, j, k inner; ses3d_init.f90:300-325) and
+    // keeps the last match. The test is a conjunction of one condition per axis, so the
+    // matches form a product set whose last element in that order is the largest matching
+    // index on each axis: three scans instead of one over all elements.
+    int im = -1, jm = -1, km = -1;
     for (int i = 0; i <= g.nx; ++i)
-      for (int j = 0; j <= g.ny; ++j)
-        for (int k = 0; k <= g.nz; ++k)
-          if (rc1 <= g.X(i, LPD) + tol && rc1 >= g.X(i, 0) - tol && rc2 <= g.Y(j, LPD) + tol &&
-              rc2 >= g.Y(j, 0) - tol && g.zmax_global - rc3 <= g.Z(k, 0) && g.zmax_global - rc3 >= g.Z(k, LPD)) {
-            r.std[0] = 2.0f * ((rc1 - g.xmin) / g.dx - (float)i) - 1.0f;
-            r.std[1] = 2.0f * ((rc2 - g.ymin) / g.dy - (float)j) - 1.0f;
-            r.std[2] = -2.0f * ((g.zmax_global - rc3 - g.zmax) / g.dz + (float)k) - 1.0f;
-            r.loc[0] = rc1; r.loc[1] = rc2; r.loc[2] = rc3;
-            r.rx = i; r.ry = j; r.rz = k;  // last matching element wins
-          }
+      if (rc1 <= g.X(i, LPD) + tol && rc1 >= g.X(i, 0) - tol) im = i;
+    for (int j = 0; j <= g.ny; ++j)
+      if (rc2 <= g.Y(j, LPD) + tol && rc2 >= g.Y(j, 0) - tol) jm = j;
+    for (int k = 0; k <= g.nz; ++k)
+      if (g.zmax_global - rc3 <= g.Z(k, 0) && g.zmax_global - rc3 >= g.Z(k, LPD)) km = k;
+    if (im >= 0 && jm >= 0 && km >= 0) {
+      r.std[0] = 2.0f * ((rc1 - g.xmin) / g.dx - (float)im) - 1.0f;
+      r.std[1] = 2.0f * ((rc2 - g.ymin) / g.dy - (float)jm) - 1.0f;
+      r.std[2] = -2.0f * ((g.zmax_global - rc3 - g.zmax) / g.dz + (float)km) - 1.0f;
+      r.loc[0] = rc1; r.loc[1] = rc2; r.loc[2] = rc3;
+      r.rx = im; r.ry = jm; r.rz = km;
+    }
     for (int i = 0; i < NP; ++i)
       for (int j = 0; j < NP; ++j)
         for (int k = 0; k < NP; ++k)
