@@ -40,7 +40,13 @@ struct ElemCtx {
   size_t N, m0;
   float *S;  // this node's state in global memory: field f at S[f * 125]
   float vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC;
+  const float *lt;  // this element's 1-D table entries in shared memory (LT_*), or null
 };
+
+// Per-element copy of the 1-D tables (five entries per axis) and the event's source
+// element, prefetched into shared memory by the persistent element kernel.
+enum { LT_SIN = 0, LT_COT = 5, LT_ISIN = 10, LT_PX = 15, LT_PY = 20, LT_R = 25, LT_IR = 30, LT_PZ = 35,
+       LT_SRC = 40, LT_FLOATS = 48 };
 
 // Element forces: component c of node n of element e at 375 e + 125 c + n of its event.
 __device__ __forceinline__ unsigned force_offset(const Consts &c, int i, int j, int k, int in, int jn, int kn) {
@@ -80,11 +86,12 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
     }
     // spherical completion (ses3d_evolution.f90:93-103), divisions by r and r sin(theta)
     // taken as products with the tabulated reciprocals
-    r = __ldg(p.r_z + k * 5 + kn);
-    st = __ldg(p.sin_x + ii * 5 + in);
-    const float ir = __ldg(p.inv_r + k * 5 + kn);
-    const float irs = ir * __ldg(p.inv_sin + ii * 5 + in);
-    const float ct = __ldg(p.cot_x + ii * 5 + in);
+    const float *lt = x.lt;
+    r = lt ? lt[LT_R + kn] : __ldg(p.r_z + k * 5 + kn);
+    st = lt ? lt[LT_SIN + in] : __ldg(p.sin_x + ii * 5 + in);
+    const float ir = lt ? lt[LT_IR + kn] : __ldg(p.inv_r + k * 5 + kn);
+    const float irs = ir * (lt ? lt[LT_ISIN + in] : __ldg(p.inv_sin + ii * 5 + in));
+    const float ct = lt ? lt[LT_COT + in] : __ldg(p.cot_x + ii * 5 + in);
     ezz = -ezz;
     eyy = eyy * irs + (vz + vx * ct) * ir;
     exx = (vz + exx) * ir;
@@ -106,7 +113,9 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
       S[F_DZUX * 125] = dzux; S[F_DYUZ * 125] = dyuz; S[F_DZUY * 125] = dzuy;
     }
     // PML profiles of this node (ses3d_init.f90:678-686), corners normalised
-    const float pxr = __ldg(p.pxr + ii * 5 + in), pyr = __ldg(p.pyr + j * 5 + jn), pzr = __ldg(p.pzr + k * 5 + kn);
+    const float pxr = lt ? lt[LT_PX + in] : __ldg(p.pxr + ii * 5 + in);
+    const float pyr = lt ? lt[LT_PY + jn] : __ldg(p.pyr + j * 5 + jn);
+    const float pzr = lt ? lt[LT_PZ + kn] : __ldg(p.pzr + k * 5 + kn);
     float px = 0.f, py = 0.f, pz = 0.f, taper = 1.f;
     const float praw = __fadd_rn(__fadd_rn(pxr, pyr), pzr);
     if (praw != 0.f) {
@@ -184,7 +193,7 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
     S[F_SXY * 125] = s_xy * taper; S[F_SXZ * 125] = s_xz * taper; S[F_SYZ * 125] = s_yz * taper;
     if (full) { S[F_SYX * 125] = s_yx * taper; S[F_SZX * 125] = s_zx * taper; S[F_SZY * 125] = s_zy * taper; }
     // moment-tensor source field (ses3d_miscellaneous.f90:115-147)
-    if (MODE != 2 && (int)e == __ldg(p.src_elem + ev)) {
+    if (MODE != 2 && (int)e == (lt ? __float_as_int(lt[LT_SRC]) : __ldg(p.src_elem + ev))) {
       const int it = *p.d_it + 1;
       const float d = p.src_delta[ev * 125 + nn];
       const float so = p.stf[(size_t)ev * c.nt + (it - 1)];
@@ -359,7 +368,7 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
   }
   s_v[sub][0][n] = vx; s_v[sub][1][n] = vy; s_v[sub][2][n] = vz;
   __syncthreads();
-  ElemCtx x{act, full, n, nn, in, jn, kn, ii, j, k, ev, e, N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC};
+  ElemCtx x{act, full, n, nn, in, jn, kn, ii, j, k, ev, e, N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC, nullptr};
   element_compute<DISS, MODE>(c, p, tab, s_v[sub], s_p[sub], x, sv);
 }
 
@@ -394,8 +403,9 @@ struct __align__(16) ElemStage {
   float state[ELEM_STATE];  // 18,000 B
   float mat[ELEM_MAT];      // 3,072 B
 };
-constexpr size_t TMA_BAR_OFF =
+constexpr size_t TMA_LT_OFF =
     TMA_STAGES * sizeof(ElemStage) + (9 + 3 * TMA_VBUF) * TPE * sizeof(float) + ((sizeof(KTab) + 15) / 16) * 16;
+constexpr size_t TMA_BAR_OFF = TMA_LT_OFF + TMA_VBUF * LT_FLOATS * sizeof(float);
 constexpr size_t TMA_SMEM = TMA_BAR_OFF + TMA_STAGES * sizeof(unsigned long long);
 
 __device__ __forceinline__ unsigned smem_addr(const void *ptr) { return (unsigned)__cvta_generic_to_shared(ptr); }
@@ -484,19 +494,40 @@ __device__ __forceinline__ void issue_item(const Consts &c, const Ptrs &p, long 
 
 // Element-local velocity of one item gathered from the assembled field straight into
 // shared memory with 4-byte cp.async (ses3d_evolution.f90:27-51); one commit group.
-__device__ __forceinline__ void gather_v_async(const Consts &c, const Ptrs &p, long long item, float (*dst)[TPE], int n,
-                                               int in, int jn, int kn) {
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+// The element-local velocity and, with TABLES, the item's 1-D table entries and source
+// element into lt (threads 0..15), in one commit group. (The table copies pay off in
+// lean iterations; with the full state they cost more than the loads they replace.)
+template <bool TABLES>
+__device__ __forceinline__ void gather_v_async(const Consts &c, const Ptrs &p, long long item, float (*dst)[TPE],
+                                               float *lt, int n, int in, int jn, int kn) {
+  const int ev = (int)(item % c.nev);
+  const unsigned e = (unsigned)(item / c.nev);
+  const int i = (int)(e % (unsigned)c.ex), j = (int)((e / (unsigned)c.ex) % (unsigned)c.ey);
+  const int k = (int)(e / ((unsigned)c.ex * (unsigned)c.ey));
   if (n < 125) {
-    const int ev = (int)(item % c.nev);
-    const unsigned e = (unsigned)(item / c.nev);
-    const int i = (int)(e % (unsigned)c.ex), j = (int)((e / (unsigned)c.ex) % (unsigned)c.ey);
-    const int k = (int)(e / ((unsigned)c.ex * (unsigned)c.ey));
     const size_t g = (size_t)(i * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
     const float *v = p.v + (size_t)ev * 3 * c.G + g;
 #pragma unroll
-    for (int q = 0; q < 3; ++q)
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(&dst[q][n])), "l"(v + (size_t)q * c.G)
-                   : "memory");
+    for (int q = 0; q < 3; ++q) cp_async4(&dst[q][n], v + (size_t)q * c.G);
+  }
+  if (!TABLES) {
+  } else if (n < 5) {
+    cp_async4(lt + LT_SIN + n, p.sin_x + i * 5 + n);
+    cp_async4(lt + LT_COT + n, p.cot_x + i * 5 + n);
+    cp_async4(lt + LT_ISIN + n, p.inv_sin + i * 5 + n);
+    cp_async4(lt + LT_PX + n, p.pxr + i * 5 + n);
+  } else if (n < 10) {
+    cp_async4(lt + LT_PY + (n - 5), p.pyr + j * 5 + (n - 5));
+  } else if (n < 15) {
+    cp_async4(lt + LT_R + (n - 10), p.r_z + k * 5 + (n - 10));
+    cp_async4(lt + LT_IR + (n - 10), p.inv_r + k * 5 + (n - 10));
+    cp_async4(lt + LT_PZ + (n - 10), p.pzr + k * 5 + (n - 10));
+  } else if (n == 15) {
+    cp_async4(lt + LT_SRC, p.src_elem + ev);
   }
   asm volatile("cp.async.commit_group;" ::: "memory");
 }
@@ -508,6 +539,7 @@ __global__ void __launch_bounds__(TPE, SES3D_TMA_MINB) k_element_tma(const Const
   float (*s_vb)[TPE] = reinterpret_cast<float (*)[TPE]>(smem + TMA_STAGES * sizeof(ElemStage));  // [TMA_VBUF][3]
   float (*s_p)[TPE] = s_vb + 3 * TMA_VBUF;
   KTab *tab = reinterpret_cast<KTab *>(s_p + 9);
+  float *s_lt = reinterpret_cast<float *>(smem + TMA_LT_OFF);  // [TMA_VBUF][LT_FLOATS]
   unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + TMA_BAR_OFF);
 
   const int n = threadIdx.x;
@@ -528,7 +560,8 @@ __global__ void __launch_bounds__(TPE, SES3D_TMA_MINB) k_element_tma(const Const
   const bool on = n < 125;
   const int nn = on ? n : 0;
   const int in = nn % 5, jn = (nn / 5) % 5, kn = nn / 25;
-  if (TMA_VBUF == 2 && first < total) gather_v_async(c, p, first, s_vb, n, in, jn, kn);
+  constexpr bool TABLES = MODE == 3;
+  if (TMA_VBUF == 2 && first < total) gather_v_async<TABLES>(c, p, first, s_vb, s_lt, n, in, jn, kn);
   for (int t = 0;; ++t) {
     const long long item = first + (long long)t * stride;
     if (item >= total) break;
@@ -586,7 +619,9 @@ __global__ void __launch_bounds__(TPE, SES3D_TMA_MINB) k_element_tma(const Const
     }
     // stage s fully read, s_v complete; the other velocity buffer was last read before the
     // previous item's divergence barrier
-    if (TMA_VBUF == 2 && item + stride < total) gather_v_async(c, p, item + stride, s_vb + 3 * ((t + 1) % 2), n, in, jn, kn);
+    if (TMA_VBUF == 2 && item + stride < total)
+      gather_v_async<TABLES>(c, p, item + stride, s_vb + 3 * ((t + 1) % 2), s_lt + LT_FLOATS * ((t + 1) % 2), n, in,
+                             jn, kn);
     if (n == 0) {
       const long long next = item + TMA_STAGES * stride;
       if (next < total) {
@@ -596,7 +631,8 @@ __global__ void __launch_bounds__(TPE, SES3D_TMA_MINB) k_element_tma(const Const
     }
     const size_t m0 = (size_t)e * 125 + nn;
     float *S = p.state + ((size_t)ev * c.E + e) * ELEM_STATE + nn;
-    ElemCtx x{on, full, n, nn, in, jn, kn, i, j, k, ev, e, (size_t)c.N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC};
+    const float *lt = (TMA_VBUF == 2 && TABLES) ? s_lt + LT_FLOATS * (t % 2) : nullptr;
+    ElemCtx x{on, full, n, nn, in, jn, kn, i, j, k, ev, e, (size_t)c.N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC, lt};
     element_compute<DISS, (MODE == 3 ? 3 : 0)>(c, p, *tab, s_v, s_p, x, sv);
   }
 }
