@@ -189,18 +189,9 @@ def run_ours(args, rank, world, local):
     sim.set_lean(args.lean)
     if args.epb:
         sim.set_block_elements(args.epb)
-    else:  # autotune the element-kernel block shape on a few steps
-        best = None
-        for epb in (1, 2, 4):
-            sim.set_block_elements(epb)
-            sim.profile(True)
-            sim.step(2)
-            ms, n = sim.kernel_time("element")
-            if best is None or ms / n < best[1]:
-                best = (epb, ms / n)
-        sim.profile(False)
-        sim.set_block_elements(best[0])
-        args.epb = best[0]
+    else:  # the library's block-shape autotuner, on a few warm-up steps
+        tuned = sim.autotune(steps_each=2)
+        args.epb = min(tuned, key=tuned.get)
     if args.graph:
         sim.use_graph(True, args.graph)
     # warm-up (the autotune steps above count towards it)

@@ -160,6 +160,27 @@ class Simulation:
     def set_block_elements(self, n: int):
         self._check(self.lib.ses3d_gpu_set_block_elements(self.h, int(n)))
 
+    def autotune(self, steps_each: int = 2, candidates=(1, 2, 4)) -> dict:
+        """Block-shape autotuner: times the element kernel (CUDA events) over `steps_each`
+        real iterations per candidate elements-per-CTA (1 = the persistent bulk-copy kernel,
+        2 and 4 = the register-staged kernel), keeps the fastest and returns
+        {candidate: ms per launch}. The iterations it spends are part of the run (the time
+        axis advances), so call it during warm-up; candidates without steps_each iterations
+        left are skipped."""
+        timings = {}
+        for epb in candidates:
+            if self.nt - self.it < steps_each:
+                break
+            self.set_block_elements(epb)
+            self.profile(True)
+            self.step(steps_each)
+            ms, n = self.kernel_time("element")
+            timings[epb] = ms / max(n, 1)
+        self.profile(False)
+        if timings:
+            self.set_block_elements(min(timings, key=timings.get))
+        return timings
+
     def begin_adjoint(self):
         self._check(self.lib.ses3d_gpu_begin_adjoint(self.h))
         self.cfg.adjoint_flag = 2

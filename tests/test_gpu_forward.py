@@ -261,3 +261,18 @@ def test_watchdog_and_errors(native):
         with pytest.raises(_lib.Ses3dError) as ei:
             sim.vmax()
         assert ei.value.code == -5
+
+
+def test_autotune_picks_a_candidate_and_keeps_results(native):
+    """The block-shape autotuner steps the run forward on each candidate and leaves the
+    fastest selected; the results equal an untuned run bit for bit."""
+    from ses3d_gb300.solver import Simulation
+    p = synth.make_problem("tiny", nt=30, seed=8)
+    with Simulation.from_problem(p) as a:
+        tuned = a.autotune(steps_each=2)
+        assert set(tuned) == {1, 2, 4} and a.it == 6 and all(v > 0 for v in tuned.values())
+        a.run()
+        va = a.field("vz_global")
+    with Simulation.from_problem(p) as b:
+        b.run()
+        assert np.array_equal(va, b.field("vz_global"))
