@@ -54,9 +54,16 @@ __device__ __forceinline__ unsigned force_offset(const Consts &c, int i, int j, 
          (unsigned)(in + 5 * jn + 25 * kn);
 }
 
-template <bool DISS, int MODE>
+struct NoHook {
+  __device__ void operator()() const {}
+};
+
+// after_barrier() runs on every thread right after the barrier between the stress and
+// divergence phases (the persistent kernel issues its next bulk copies there).
+template <bool DISS, int MODE, class Hook = NoHook>
 __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, const KTab &tab, float (*s_v)[TPE],
-                                                float (*s_p)[TPE], const ElemCtx &x, float *sv) {
+                                                float (*s_p)[TPE], const ElemCtx &x, float *sv,
+                                                const Hook &after_barrier = Hook()) {
   constexpr int NS = DISS ? NSTATE : 18;
   const bool act = x.act, full = x.full;
   const int n = x.n, nn = x.nn, in = x.in, jn = x.jn, kn = x.kn, ii = x.ii, j = x.j, k = x.k, ev = x.ev;
@@ -260,6 +267,7 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
     }
   }
   __syncthreads();
+  after_barrier();
 
   if (act) {
     // weak-form divergence (ses3d_evolution.f90:235-270)
@@ -622,18 +630,25 @@ __global__ void __launch_bounds__(TPE, SES3D_TMA_MINB) k_element_tma(const Const
     if (TMA_VBUF == 2 && item + stride < total)
       gather_v_async<TABLES>(c, p, item + stride, s_vb + 3 * ((t + 1) % 2), s_lt + LT_FLOATS * ((t + 1) % 2), n, in,
                              jn, kn);
-    if (n == 0) {
-      const long long next = item + TMA_STAGES * stride;
-      if (next < total) {
+    const long long refill = item + TMA_STAGES * stride;
+    auto issue_refill = [&]() {
+      if (n == 0 && refill < total) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        issue_item<DISS, MODE>(c, p, next, &stage[s], &bar[s]);
+        issue_item<DISS, MODE>(c, p, refill, &stage[s], &bar[s]);
       }
-    }
+    };
+    // When to issue the next item's bulk copy (measured on 96 x 96 x 40): lean items are
+    // short, so right after this item's state has been read; full-state items after the
+    // stress/divergence barrier, which keeps thread 0's copy work off that barrier
+    // (2.65 -> 2.42 ms per launch), while lean iterations lose 6 % that way.
+    constexpr bool LATE_REFILL = MODE != 3;
+    if (!LATE_REFILL) issue_refill();
     const size_t m0 = (size_t)e * 125 + nn;
     float *S = p.state + ((size_t)ev * c.E + e) * ELEM_STATE + nn;
     const float *lt = (TMA_VBUF == 2 && TABLES) ? s_lt + LT_FLOATS * (t % 2) : nullptr;
     ElemCtx x{on, full, n, nn, in, jn, kn, i, j, k, ev, e, (size_t)c.N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC, lt};
-    element_compute<DISS, (MODE == 3 ? 3 : 0)>(c, p, *tab, s_v, s_p, x, sv);
+    if (LATE_REFILL) element_compute<DISS, (MODE == 3 ? 3 : 0)>(c, p, *tab, s_v, s_p, x, sv, issue_refill);
+    else element_compute<DISS, (MODE == 3 ? 3 : 0)>(c, p, *tab, s_v, s_p, x, sv);
   }
 }
 
