@@ -167,6 +167,11 @@ int ses3d_gpu_get_kernel(ses3d_gpu *h, int event, int which, double *out);
  * transfer. */
 int ses3d_gpu_get_kernel_sum(ses3d_gpu *h, int which, double *out);
 
+/* The same sum written to device memory (N doubles on the handle's device, reference
+ * layout), for callers that keep the gradient on the GPU (PyTorch). No counterpart in the
+ * reference. */
+int ses3d_gpu_get_kernel_sum_device(ses3d_gpu *h, int which, double *out);
+
 /* Forward-field records kept in device memory by an adjoint_flag == 1 run: one
  * record per stored iteration (it == 1, it % samp_ad == 0, it == nt), 9 fields of
  * N floats each: vx, vy, vz, exx, eyy, ezz, exy, exz, eyz -- the fields and order of

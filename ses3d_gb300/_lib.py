@@ -67,6 +67,7 @@ SIGNATURES = {
     "ses3d_gpu_set_field": (c_int, [c_void_p, c_int, c_int, P_f]),
     "ses3d_gpu_get_kernel": (c_int, [c_void_p, c_int, c_int, P_d]),
     "ses3d_gpu_get_kernel_sum": (c_int, [c_void_p, c_int, P_d]),
+    "ses3d_gpu_get_kernel_sum_device": (c_int, [c_void_p, c_int, c_void_p]),
     "ses3d_gpu_selftest_wait": (c_int, [c_void_p, c_int]),
     "ses3d_gpu_record_count": (c_int, [c_void_p, c_int]),
     "ses3d_gpu_get_record": (c_int, [c_void_p, c_int, c_int, P_f]),

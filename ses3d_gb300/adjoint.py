@@ -275,6 +275,34 @@ def quadrature_volume(sim: Simulation):
     return out.reshape(-1), jac
 
 
+def quadrature_volume_device(sim: Simulation, device):
+    """quadrature_volume as an FP64 torch tensor on `device` (same operation order)."""
+    import torch
+    c = sim.cfg
+    ex, ey, ez = c.nx + 1, c.ny + 1, c.nz + 1
+    f64 = dict(dtype=torch.float64, device=device)
+    w = torch.tensor(sim.setup_real("w").astype(np.float64), **f64)
+    jac = float(sim.setup_real("Jac")[0])
+    x = torch.tensor(sim.setup_real("x").astype(np.float64), **f64).reshape(5, ex)   # [in, i]
+    z = torch.tensor(sim.setup_real("z").astype(np.float64), **f64).reshape(5, ez)   # [kn, k]
+    sin, r2 = torch.sin(x), z * z
+    coef = w[None, None, :] * w[None, :, None] * w[:, None, None] * jac             # [kn, jn, in]
+    out = coef[:, :, :, None, None, None] * r2[:, None, None, :, None, None] * sin[None, None, :, None, None, :]
+    return out.expand(5, 5, 5, ez, ey, ex).reshape(-1), jac
+
+
+def kernel_sums_device(sim: Simulation, device) -> list:
+    """Event-summed kernels of KERNEL_NAMES as FP64 tensors on `device` (no host copy)."""
+    import torch
+    out = []
+    for nm in KERNEL_NAMES:
+        t = torch.empty(sim.N, dtype=torch.float64, device=device)
+        torch.cuda.synchronize(device)
+        sim.kernel_sum_device(nm, t.data_ptr())   # returns after the library's stream finished
+        out.append(t)
+    return out
+
+
 KERNEL_NAMES = ("rho", "cp", "csh", "csv", "Q_mu")
 
 
@@ -312,8 +340,8 @@ class _Misfit:
                         sim.begin_adjoint()
                         sim.run()
                         if W is None:
-                            W, jac = quadrature_volume(sim)
-                        part = [sim.kernel_sum(nm) for nm in KERNEL_NAMES]   # events in index order
+                            W, jac = quadrature_volume_device(sim, rho.device)
+                        part = kernel_sums_device(sim, rho.device)            # events in index order
                         ksum = part if ksum is None else [a + b for a, b in zip(ksum, part)]
                         sim.close()
                         syn += sg
@@ -333,16 +361,15 @@ class _Misfit:
                         sim.set_adjoint_sources(k, e.recloc, srcs[k])
                     sim.begin_adjoint()
                     sim.run()
-                    W, jac = quadrature_volume(sim)
-                    ksum = [sim.kernel_sum(nm) for nm in KERNEL_NAMES]
+                    W, jac = quadrature_volume_device(sim, Q.device)
+                    ksum = kernel_sums_device(sim, Q.device)
                     sim.close()
                     ctx.sim = None
                 else:
                     ksum, W, jac = ctx.kernels
                 # ses3d's kernel sign convention: dchi = -Jac sum W K dm (checked against FD)
                 scale = -float(grad_out) * jac
-                dev = Q.device
-                grads = [torch.from_numpy(k * W * scale).to(dev) for k in ksum]
+                grads = [k * W * scale for k in ksum]
                 grads[4] = grads[4] / Q.double()
                 setup.last["kernels"] = {n: g for n, g in zip(("rho", "vp", "vsh", "vsv", "Q"), grads)}
                 return (None,) + tuple(g.to(Q.dtype) for g in grads)

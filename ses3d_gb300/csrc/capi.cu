@@ -982,17 +982,19 @@ int ses3d_gpu_get_kernel(ses3d_gpu *h, int event, int which, double *out) {
   return SES3D_OK;
 }
 
-int ses3d_gpu_get_kernel_sum(ses3d_gpu *h, int which, double *out) {
+// Event sum of one kernel into out (reference layout): host memory, or device memory of
+// the handle's device when `device` is set (no host copy).
+static int kernel_sum(ses3d_gpu *h, int which, double *out, bool device) {
   if (!h) return SES3D_E_CONFIG;
   if (which < 0 || which >= SES3D_KERNEL_COUNT || !out) return fail(h, SES3D_E_CONFIG, "bad kernel id");
   if (!h->d_grad) return fail(h, SES3D_E_STATE, "kernels exist only in adjoint runs (adjoint_flag = 2)");
   const long long N = h->geo.N;
   double *tmp = nullptr, *sum = nullptr;
-  CK(h, dalloc(&tmp, (size_t)N));
-  cudaError_t e = dalloc(&sum, (size_t)N);
+  CK(h, dalloc(&sum, (size_t)N));
+  cudaError_t e = device ? cudaSuccess : dalloc(&tmp, (size_t)N);
   if (e == cudaSuccess) e = launch_sum_events_d(h->d_grad, which, h->cfg.n_events, N, sum, h->st);
-  if (e == cudaSuccess) e = launch_transpose_d(sum, tmp, h->geo.E, NPE, h->st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(out, tmp, N * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+  if (e == cudaSuccess) e = launch_transpose_d(sum, device ? out : tmp, h->geo.E, NPE, h->st);
+  if (e == cudaSuccess && !device) e = cudaMemcpyAsync(out, tmp, N * sizeof(double), cudaMemcpyDeviceToHost, h->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
   dfree(tmp);
   dfree(sum);
@@ -1000,6 +1002,10 @@ int ses3d_gpu_get_kernel_sum(ses3d_gpu *h, int which, double *out) {
   h->launches += 2;
   return SES3D_OK;
 }
+
+int ses3d_gpu_get_kernel_sum(ses3d_gpu *h, int which, double *out) { return kernel_sum(h, which, out, false); }
+
+int ses3d_gpu_get_kernel_sum_device(ses3d_gpu *h, int which, double *out) { return kernel_sum(h, which, out, true); }
 
 int ses3d_gpu_record_count(const ses3d_gpu *h, int event) {
   if (!h || event < 0 || event >= h->cfg.n_events) return SES3D_E_CONFIG;

@@ -219,6 +219,10 @@ class Simulation:
         self._check(self.lib.ses3d_gpu_get_kernel_sum(self.h, L.KERNEL_ID[name], L.dptr(out)))
         return out
 
+    def kernel_sum_device(self, name: str, out_ptr: int):
+        """Event sum of one kernel written to device memory at out_ptr (N doubles)."""
+        self._check(self.lib.ses3d_gpu_get_kernel_sum_device(self.h, L.KERNEL_ID[name], ctypes.c_void_p(out_ptr)))
+
     def record_count(self, event: int = 0) -> int:
         return self._check(self.lib.ses3d_gpu_record_count(self.h, event))
 
