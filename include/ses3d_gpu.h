@@ -172,6 +172,22 @@ int ses3d_gpu_get_kernel_sum(ses3d_gpu *h, int which, double *out);
  * reference. */
 int ses3d_gpu_get_kernel_sum_device(ses3d_gpu *h, int which, double *out);
 
+/* acc[q] = acc[q] + (the event sum of get_kernel_sum_device) on the handle's device: sums
+ * of event sub-batches run in separate handles, added in sub-batch order. No counterpart
+ * in the reference (its per-event grad_* files are summed afterwards). */
+int ses3d_gpu_add_kernel_sum_device(ses3d_gpu *h, int which, double *acc);
+
+/* Misfit gradient with respect to a model record from an event-summed kernel (N doubles,
+ * reference layout, device memory): out[q] = (ksum[q] * W[q]) * (scale * Jac), divided by
+ * divisor[q] when divisor is not NULL, where W[q] = w_in w_jn w_kn Jac r^2 sin(theta) is the
+ * quadrature volume of GLL point q of cfg's box (FP64). With ses3d's kernel convention
+ * (grad_* carry 1/Jac, SOURCE/ses3d_grad.f90:77-83) and scale = -dL/dchi this is dL/dm;
+ * the Q_mu kernel takes divisor = Q. out and divisor are FP32 (f64 = 0) or FP64 (f64 = 1),
+ * N values. Needs no handle (the handles of event sub-batches may be gone); runs on the
+ * current device of this library and returns when done. No counterpart in the reference. */
+int ses3d_gpu_misfit_gradient_device(const ses3d_config *cfg, const double *ksum, double scale,
+                                     const void *divisor, void *out, int f64);
+
 /* Forward-field records kept in device memory by an adjoint_flag == 1 run: one
  * record per stored iteration (it == 1, it % samp_ad == 0, it == nt), 9 fields of
  * N floats each: vx, vy, vz, exx, eyy, ezz, exy, exz, eyz -- the fields and order of

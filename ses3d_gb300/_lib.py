@@ -68,6 +68,9 @@ SIGNATURES = {
     "ses3d_gpu_get_kernel": (c_int, [c_void_p, c_int, c_int, P_d]),
     "ses3d_gpu_get_kernel_sum": (c_int, [c_void_p, c_int, P_d]),
     "ses3d_gpu_get_kernel_sum_device": (c_int, [c_void_p, c_int, c_void_p]),
+    "ses3d_gpu_add_kernel_sum_device": (c_int, [c_void_p, c_int, c_void_p]),
+    "ses3d_gpu_misfit_gradient_device": (c_int, [ctypes.POINTER(Config), c_void_p, ctypes.c_double, c_void_p,
+                                                 c_void_p, c_int]),
     "ses3d_gpu_selftest_wait": (c_int, [c_void_p, c_int]),
     "ses3d_gpu_record_count": (c_int, [c_void_p, c_int]),
     "ses3d_gpu_get_record": (c_int, [c_void_p, c_int, c_int, P_f]),

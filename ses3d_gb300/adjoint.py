@@ -24,6 +24,7 @@ force applied in adjoint iteration it is the time derivative of the time-reverse
 """
 from __future__ import annotations
 
+import ctypes
 import math
 from dataclasses import dataclass, field
 from typing import List, Optional, Sequence
@@ -258,49 +259,44 @@ def ctypes_copy(dst, src):
             setattr(dst, name, v)
 
 
-def quadrature_volume(sim: Simulation):
-    """W_(e,n) = w_i w_j w_k Jac r^2 sin(theta) in the reference layout (FP64) and Jac."""
-    c = sim.cfg
-    ex, ey, ez = c.nx + 1, c.ny + 1, c.nz + 1
-    w = sim.setup_real("w").astype(np.float64)
-    jac = float(sim.setup_real("Jac")[0])
-    x = sim.setup_real("x").astype(np.float64).reshape(5, ex)   # [in, i]
-    z = sim.setup_real("z").astype(np.float64).reshape(5, ez)   # [kn, k]
-    sin, r2 = np.sin(x), z * z
-    out = np.empty((5, 5, 5, ez, ey, ex))                        # [kn, jn, in, k, j, i]
-    for kn in range(5):
-        for jn in range(5):
-            for in_ in range(5):
-                out[kn, jn, in_] = (w[in_] * w[jn] * w[kn] * jac) * r2[kn][:, None, None] * sin[in_][None, None, :]
-    return out.reshape(-1), jac
-
-
-def quadrature_volume_device(sim: Simulation, device):
-    """quadrature_volume as an FP64 torch tensor on `device` (same operation order)."""
+def kernel_sums_device(sim: Simulation, device, acc: Optional[list] = None) -> list:
+    """Event-summed kernels of KERNEL_NAMES as FP64 tensors on `device` (no host copy); with
+    `acc` (the sums of earlier event sub-batches) the sums are added to it in place."""
     import torch
-    c = sim.cfg
-    ex, ey, ez = c.nx + 1, c.ny + 1, c.nz + 1
-    f64 = dict(dtype=torch.float64, device=device)
-    w = torch.tensor(sim.setup_real("w").astype(np.float64), **f64)
-    jac = float(sim.setup_real("Jac")[0])
-    x = torch.tensor(sim.setup_real("x").astype(np.float64), **f64).reshape(5, ex)   # [in, i]
-    z = torch.tensor(sim.setup_real("z").astype(np.float64), **f64).reshape(5, ez)   # [kn, k]
-    sin, r2 = torch.sin(x), z * z
-    coef = w[None, None, :] * w[None, :, None] * w[:, None, None] * jac             # [kn, jn, in]
-    out = coef[:, :, :, None, None, None] * r2[:, None, None, :, None, None] * sin[None, None, :, None, None, :]
-    return out.expand(5, 5, 5, ez, ey, ex).reshape(-1), jac
-
-
-def kernel_sums_device(sim: Simulation, device) -> list:
-    """Event-summed kernels of KERNEL_NAMES as FP64 tensors on `device` (no host copy)."""
-    import torch
+    torch.cuda.synchronize(device)
     out = []
-    for nm in KERNEL_NAMES:
-        t = torch.empty(sim.N, dtype=torch.float64, device=device)
-        torch.cuda.synchronize(device)
-        sim.kernel_sum_device(nm, t.data_ptr())   # returns after the library's stream finished
+    for i, nm in enumerate(KERNEL_NAMES):
+        if acc is None:
+            t = torch.empty(sim.N, dtype=torch.float64, device=device)
+            sim.kernel_sum_device(nm, t.data_ptr())   # returns after the library's stream finished
+        else:
+            t = acc[i]
+            sim.add_kernel_sum_device(nm, t.data_ptr())
         out.append(t)
     return out
+
+
+def misfit_gradients_device(cfg: L.Config, ksum: list, grad_out: float, Q) -> list:
+    """dL/dm for (rho, vp, vsh, vsv, Q) from the event-summed kernels, in Q's dtype on Q's
+    device: (K * W) * (-grad_out * Jac) with W the quadrature volume of each GLL point, the
+    Q_mu one divided by Q (ses3d's kernel sign convention: dchi = -Jac sum W K dm, checked
+    against finite differences). One library kernel per model record."""
+    import torch
+    if Q.dtype not in (torch.float32, torch.float64):
+        raise TypeError("model tensors must be float32 or float64")
+    lib = L.load()
+    f64 = int(Q.dtype == torch.float64)
+    q = Q.detach().contiguous()
+    torch.cuda.synchronize(Q.device)
+    grads = []
+    for i, k in enumerate(ksum):
+        g = torch.empty(q.shape, dtype=Q.dtype, device=Q.device)
+        L.check(lib.ses3d_gpu_misfit_gradient_device(ctypes.byref(cfg), ctypes.c_void_p(k.data_ptr()),
+                                                       -float(grad_out),
+                                                       ctypes.c_void_p(q.data_ptr()) if i == 4 else None,
+                                                       ctypes.c_void_p(g.data_ptr()), f64))
+        grads.append(g)
+    return grads
 
 
 KERNEL_NAMES = ("rho", "cp", "csh", "csv", "Q_mu")
@@ -330,7 +326,7 @@ class _Misfit:
                     # sub-batches: an event's adjoint sources depend on its own residual only,
                     # so each sub-batch runs forward, adjoint and kernel sum here and is freed;
                     # backward scales the summed kernels
-                    syn, ksum, W, jac = [], None, None, None
+                    syn, ksum = [], None
                     for grp in plan.groups:
                         sim = setup.simulate(recs, adjoint=True, events=grp, K=plan.K)
                         sg = setup.seismograms(sim)
@@ -339,13 +335,10 @@ class _Misfit:
                             sim.set_adjoint_sources(slot, setup.events[k].recloc, srcs[slot])
                         sim.begin_adjoint()
                         sim.run()
-                        if W is None:
-                            W, jac = quadrature_volume_device(sim, rho.device)
-                        part = kernel_sums_device(sim, rho.device)            # events in index order
-                        ksum = part if ksum is None else [a + b for a, b in zip(ksum, part)]
+                        ksum = kernel_sums_device(sim, rho.device, ksum)   # events in index order
                         sim.close()
                         syn += sg
-                    ctx.sim, ctx.syn, ctx.kernels = None, syn, (ksum, W, jac)
+                    ctx.sim, ctx.syn, ctx.kernels = None, syn, ksum
                 chi = setup.misfit_value(syn, dt)
                 setup.last["seismograms"] = syn
                 return torch.tensor(chi, dtype=torch.float64, device=rho.device)
@@ -361,18 +354,14 @@ class _Misfit:
                         sim.set_adjoint_sources(k, e.recloc, srcs[k])
                     sim.begin_adjoint()
                     sim.run()
-                    W, jac = quadrature_volume_device(sim, Q.device)
                     ksum = kernel_sums_device(sim, Q.device)
                     sim.close()
                     ctx.sim = None
                 else:
-                    ksum, W, jac = ctx.kernels
-                # ses3d's kernel sign convention: dchi = -Jac sum W K dm (checked against FD)
-                scale = -float(grad_out) * jac
-                grads = [k * W * scale for k in ksum]
-                grads[4] = grads[4] / Q.double()
+                    ksum = ctx.kernels
+                grads = misfit_gradients_device(setup.cfg_template, ksum, float(grad_out), Q)
                 setup.last["kernels"] = {n: g for n, g in zip(("rho", "vp", "vsh", "vsv", "Q"), grads)}
-                return (None,) + tuple(g.to(Q.dtype) for g in grads)
+                return (None,) + tuple(grads)
 
         return WaveformMisfit
 

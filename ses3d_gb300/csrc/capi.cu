@@ -31,7 +31,10 @@ cudaError_t launch_receivers(const Consts &c, const float *v, const int *rec_ele
 cudaError_t launch_inject(const Consts &c, float *f, const int4 *groups, int ngroups, const float *delta,
                           const float *stf, const int *mask, const int *d_it, cudaStream_t st);
 cudaError_t launch_transpose(const float *in, float *out, long long rows, long long cols, cudaStream_t st);
-cudaError_t launch_transpose_d(const double *in, double *out, long long rows, long long cols, cudaStream_t st);
+cudaError_t launch_transpose_d(const double *in, double *out, long long rows, long long cols, bool accumulate,
+                               cudaStream_t st);
+cudaError_t launch_misfit_gradient(const double *K, const double *tables, int ex, int ey, int ez, double s,
+                                   const void *div, void *out, bool f64, cudaStream_t st);
 cudaError_t launch_derive(const float *raw, float *mat, float *gm, long long N, int is_diss, float sum_D_p,
                           cudaStream_t st);
 cudaError_t launch_mass(const Consts &c, const float *rhoinv, const float *z, const float *sinx, const float *w,
@@ -974,7 +977,8 @@ int ses3d_gpu_get_kernel(ses3d_gpu *h, int event, int which, double *out) {
   static const int slot[] = {0, 1, 2, 3, 4, 5, 6, 7};
   double *tmp = nullptr;
   CK(h, dalloc(&tmp, (size_t)N));
-  cudaError_t e = launch_transpose_d(h->d_grad + ((size_t)event * NGRAD + slot[which]) * N, tmp, h->geo.E, NPE, h->st);
+  cudaError_t e = launch_transpose_d(h->d_grad + ((size_t)event * NGRAD + slot[which]) * N, tmp, h->geo.E, NPE, false,
+                                     h->st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, tmp, N * sizeof(double), cudaMemcpyDeviceToHost, h->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
   dfree(tmp);
@@ -983,8 +987,9 @@ int ses3d_gpu_get_kernel(ses3d_gpu *h, int event, int which, double *out) {
 }
 
 // Event sum of one kernel into out (reference layout): host memory, or device memory of
-// the handle's device when `device` is set (no host copy).
-static int kernel_sum(ses3d_gpu *h, int which, double *out, bool device) {
+// the handle's device when `device` is set (no host copy); `accumulate` (device only) adds
+// the sum to out's values.
+static int kernel_sum(ses3d_gpu *h, int which, double *out, bool device, bool accumulate = false) {
   if (!h) return SES3D_E_CONFIG;
   if (which < 0 || which >= SES3D_KERNEL_COUNT || !out) return fail(h, SES3D_E_CONFIG, "bad kernel id");
   if (!h->d_grad) return fail(h, SES3D_E_STATE, "kernels exist only in adjoint runs (adjoint_flag = 2)");
@@ -993,7 +998,7 @@ static int kernel_sum(ses3d_gpu *h, int which, double *out, bool device) {
   CK(h, dalloc(&sum, (size_t)N));
   cudaError_t e = device ? cudaSuccess : dalloc(&tmp, (size_t)N);
   if (e == cudaSuccess) e = launch_sum_events_d(h->d_grad, which, h->cfg.n_events, N, sum, h->st);
-  if (e == cudaSuccess) e = launch_transpose_d(sum, device ? out : tmp, h->geo.E, NPE, h->st);
+  if (e == cudaSuccess) e = launch_transpose_d(sum, device ? out : tmp, h->geo.E, NPE, device && accumulate, h->st);
   if (e == cudaSuccess && !device) e = cudaMemcpyAsync(out, tmp, N * sizeof(double), cudaMemcpyDeviceToHost, h->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
   dfree(tmp);
@@ -1006,6 +1011,46 @@ static int kernel_sum(ses3d_gpu *h, int which, double *out, bool device) {
 int ses3d_gpu_get_kernel_sum(ses3d_gpu *h, int which, double *out) { return kernel_sum(h, which, out, false); }
 
 int ses3d_gpu_get_kernel_sum_device(ses3d_gpu *h, int which, double *out) { return kernel_sum(h, which, out, true); }
+
+int ses3d_gpu_add_kernel_sum_device(ses3d_gpu *h, int which, double *acc) {
+  return kernel_sum(h, which, acc, true, true);
+}
+
+int ses3d_gpu_misfit_gradient_device(const ses3d_config *cfg, const double *ksum, double scale, const void *divisor,
+                                     void *out, int f64) {
+  Range range_("ses3d misfit gradient");
+  if (!cfg || !ksum || !out) return fail(nullptr, SES3D_E_CONFIG, "null argument");
+  if (cfg->lpd != LPD) return fail(nullptr, SES3D_E_CONFIG, "this library implements lpd = 4 only");
+  Geometry g;
+  std::string msg = build_geometry(g, cfg->nx, cfg->ny, cfg->nz, cfg->pml, cfg->xmin, cfg->xmax, cfg->ymin, cfg->ymax,
+                                   cfg->zmin, cfg->zmax, cfg->zmax_global);
+  if (!msg.empty()) return fail(nullptr, SES3D_E_CONFIG, msg);
+  // FP64 tables of the quadrature volume: coef[kn][jn][in] = ((w_in w_jn) w_kn) Jac,
+  // r2[kn][k] = r^2, sinx[in][i] = sin(theta) (theta, r the FP32 GLL coordinates)
+  std::vector<double> tab((size_t)NPE + (size_t)NP * g.ez + (size_t)NP * g.ex);
+  const double jac = (double)g.Jac;
+  for (int kn = 0; kn < NP; ++kn)
+    for (int jn = 0; jn < NP; ++jn)
+      for (int in = 0; in < NP; ++in)
+        tab[(kn * NP + jn) * NP + in] = (((double)g.w[in] * (double)g.w[jn]) * (double)g.w[kn]) * jac;
+  double *r2 = tab.data() + NPE, *sinx = r2 + (size_t)NP * g.ez;
+  for (int kn = 0; kn < NP; ++kn)
+    for (int k = 0; k < g.ez; ++k) {
+      const double z = (double)g.Z(k, kn);
+      r2[(size_t)kn * g.ez + k] = z * z;
+    }
+  for (int in = 0; in < NP; ++in)
+    for (int i = 0; i < g.ex; ++i) sinx[(size_t)in * g.ex + i] = std::sin((double)g.X(i, in));
+  double *d_tab = nullptr;
+  cudaError_t e = dalloc(&d_tab, tab.size());
+  if (e == cudaSuccess) e = cudaMemcpy(d_tab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = launch_misfit_gradient(ksum, d_tab, g.ex, g.ey, g.ez, scale * jac, divisor, out, f64 != 0, 0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+  dfree(d_tab);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "misfit_gradient");
+  return SES3D_OK;
+}
 
 int ses3d_gpu_record_count(const ses3d_gpu *h, int event) {
   if (!h || event < 0 || event >= h->cfg.n_events) return SES3D_E_CONFIG;

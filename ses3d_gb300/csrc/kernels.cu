@@ -830,6 +830,8 @@ __global__ void k_transpose(const float *__restrict__ in, float *__restrict__ ou
   }
 }
 
+// ACC: out += transposed in (out's old value first), else out = transposed in.
+template <bool ACC>
 __global__ void k_transpose_d(const double *__restrict__ in, double *__restrict__ out, long long rows, long long cols) {
   __shared__ double tile[32][33];
   const long long c0 = (long long)blockIdx.x * 32, r0 = (long long)blockIdx.y * 32;
@@ -840,8 +842,37 @@ __global__ void k_transpose_d(const double *__restrict__ in, double *__restrict_
   __syncthreads();
   for (int t = threadIdx.y; t < 32; t += blockDim.y) {
     const long long cc = c0 + t, rr = r0 + threadIdx.x;
-    if (rr < rows && cc < cols) out[cc * rows + rr] = tile[threadIdx.x][t];
+    if (rr < rows && cc < cols) {
+      if (ACC) out[cc * rows + rr] = out[cc * rows + rr] + tile[threadIdx.x][t];
+      else out[cc * rows + rr] = tile[threadIdx.x][t];
+    }
   }
+}
+
+// ---------------------------------------------------------------------------------------
+// Misfit gradient from an event-summed kernel K (reference layout (i,j,k,in,jn,kn), FP64):
+// out[q] = (K[q] * W[q]) * s, divided by div[q] when div is given, rounded to T. W is the
+// quadrature volume w_in w_jn w_kn Jac r^2 sin(theta) of GLL point q, assembled from three
+// FP64 tables: coef[kn][jn][in] = ((w_in w_jn) w_kn) Jac, r2[kn][k] = r^2,
+// sinx[in][i] = sin(theta), as W = (coef * r2) * sinx.
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void k_misfit_gradient(const double *__restrict__ K, const double *__restrict__ coef,
+                                  const double *__restrict__ r2, const double *__restrict__ sinx, int ex, int ey,
+                                  int ez, double s, const T *__restrict__ div, T *__restrict__ out, long long N) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= N) return;
+  long long t = q;
+  const int i = (int)(t % ex); t /= ex;
+  t /= ey;                                   // j: W does not depend on it
+  const int k = (int)(t % ez); t /= ez;
+  const int in = (int)(t % 5); t /= 5;
+  const int jn = (int)(t % 5);
+  const int kn = (int)(t / 5);
+  const double W = (coef[(kn * 5 + jn) * 5 + in] * r2[(long long)kn * ez + k]) * sinx[(long long)in * ex + i];
+  double g = (K[q] * W) * s;
+  if (div) g = g / (double)div[q];
+  out[q] = (T)g;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1116,9 +1147,25 @@ cudaError_t launch_sum_events_d(const double *grad, int slot, int nev, long long
   return cudaGetLastError();
 }
 
-cudaError_t launch_transpose_d(const double *in, double *out, long long rows, long long cols, cudaStream_t st) {
+cudaError_t launch_transpose_d(const double *in, double *out, long long rows, long long cols, bool accumulate,
+                               cudaStream_t st) {
   dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
-  k_transpose_d<<<grid, dim3(32, 8), 0, st>>>(in, out, rows, cols);
+  if (accumulate) k_transpose_d<true><<<grid, dim3(32, 8), 0, st>>>(in, out, rows, cols);
+  else k_transpose_d<false><<<grid, dim3(32, 8), 0, st>>>(in, out, rows, cols);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_misfit_gradient(const double *K, const double *tables, int ex, int ey, int ez, double s,
+                                   const void *div, void *out, bool f64, cudaStream_t st) {
+  const long long N = (long long)ex * ey * ez * 125;
+  const double *coef = tables, *r2 = tables + 125, *sinx = r2 + 5LL * ez;
+  const unsigned blocks = (unsigned)((N + 255) / 256);
+  if (f64)
+    k_misfit_gradient<double><<<blocks, 256, 0, st>>>(K, coef, r2, sinx, ex, ey, ez, s, (const double *)div,
+                                                      (double *)out, N);
+  else
+    k_misfit_gradient<float><<<blocks, 256, 0, st>>>(K, coef, r2, sinx, ex, ey, ez, s, (const float *)div,
+                                                     (float *)out, N);
   return cudaGetLastError();
 }
 

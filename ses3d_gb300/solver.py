@@ -223,6 +223,10 @@ class Simulation:
         """Event sum of one kernel written to device memory at out_ptr (N doubles)."""
         self._check(self.lib.ses3d_gpu_get_kernel_sum_device(self.h, L.KERNEL_ID[name], ctypes.c_void_p(out_ptr)))
 
+    def add_kernel_sum_device(self, name: str, acc_ptr: int):
+        """Event sum of one kernel added to the N doubles in device memory at acc_ptr."""
+        self._check(self.lib.ses3d_gpu_add_kernel_sum_device(self.h, L.KERNEL_ID[name], ctypes.c_void_p(acc_ptr)))
+
     def record_count(self, event: int = 0) -> int:
         return self._check(self.lib.ses3d_gpu_record_count(self.h, event))
 

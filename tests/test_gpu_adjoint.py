@@ -151,3 +151,55 @@ def test_kernel_sum_over_events(native):
             per = [sim.kernel(name, k) for k in range(3)]
             assert all(np.abs(a).max() > 0 for a in per)
             assert np.array_equal(sim.kernel_sum(name), per[0] + per[1] + per[2]), name
+
+
+def test_device_kernel_sums_and_misfit_gradient(native):
+    """ses3d_gpu_add_kernel_sum_device adds the event sum to device memory exactly;
+    ses3d_gpu_misfit_gradient_device equals (K W)(scale Jac) [/ Q] evaluated in FP64 on the
+    host from the handle's geometry (W = w_i w_j w_k Jac r^2 sin(theta)), FP32 and FP64."""
+    torch = pytest.importorskip("torch")
+    from ses3d_gb300 import adjoint as A
+    from ses3d_gb300.solver import Simulation
+    p = synth.make_problem("tiny", nt=NT, seed=38, adjoint_flag=1, n_events=2)
+    p.setup.samp_ad = SAMP
+    with Simulation.from_problem(p, adjoint_flag=1, grad_variant=1) as sim:
+        sim.run()
+        for k in range(2):
+            loc, stf = adjoint_inputs(p, sim.seismograms(k))
+            sim.set_adjoint_sources(k, loc, stf)
+        sim.begin_adjoint()
+        sim.run()
+        host = {nm: sim.kernel_sum(nm) for nm in A.KERNEL_NAMES}
+        acc = [torch.full((sim.N,), 0.25, dtype=torch.float64, device="cuda") for _ in A.KERNEL_NAMES]
+        A.kernel_sums_device(sim, "cuda", acc)
+        for t, nm in zip(acc, A.KERNEL_NAMES):
+            assert np.array_equal(t.cpu().numpy(), 0.25 + host[nm]), nm
+        ksum = A.kernel_sums_device(sim, "cuda")
+        c = sim.cfg
+        ex, ey, ez = c.nx + 1, c.ny + 1, c.nz + 1
+        w = sim.setup_real("w").astype(np.float64)
+        jac = float(sim.setup_real("Jac")[0])
+        x = sim.setup_real("x").astype(np.float64).reshape(5, ex)
+        z = sim.setup_real("z").astype(np.float64).reshape(5, ez)
+    W = np.empty((5, 5, 5, ez, ey, ex))
+    for kn in range(5):
+        for jn in range(5):
+            for i_ in range(5):
+                W[kn, jn, i_] = (((w[i_] * w[jn]) * w[kn]) * jac) * (z[kn] * z[kn])[:, None, None] * \
+                    np.sin(x[i_])[None, None, :]
+    W = W.reshape(-1)
+    Q = p.model["Q"].astype(np.float32)
+    for dt in (torch.float32, torch.float64):
+        Qt = torch.tensor(Q, dtype=dt, device="cuda")
+        grads = A.misfit_gradients_device(sim.cfg, ksum, 2.0, Qt)
+        for i, (g, nm) in enumerate(zip(grads, A.KERNEL_NAMES)):
+            want = (host[nm] * W) * (-2.0 * jac)
+            if i == 4:
+                want = want / Q.astype(np.float64)
+            got = g.cpu().numpy()
+            assert got.dtype == (np.float32 if dt == torch.float32 else np.float64)
+            assert np.abs(want).max() > 0
+            if dt == torch.float64:
+                assert np.allclose(got, want, rtol=1e-14, atol=0), nm
+            else:
+                assert np.allclose(got, want.astype(np.float32), rtol=1e-6, atol=0), nm
