@@ -272,6 +272,34 @@ def make_event(rng, setup: F.Setup, nt: int, dt: float, depth_m: float, period: 
     return EventSpec(e, stf, rec, name)
 
 
+def homogeneous_problem(n_el=(10, 9, 6), colat=(48.0, 52.0), lon=(8.0, 12.0), r=(6071000.0, 6371000.0),
+                        nt: int = 600, dt: float = 0.1, pml: int = 3, source_type: int = 1,
+                        depth_m: float = 150000.0, rho: float = 3000.0, vp: float = 7000.0, vs: float = 4000.0,
+                        t0: float = 8.0, sigma: float = 3.0, amplitude: float = 1e15) -> Problem:
+    """Known-answer workload: an elastic homogeneous box (rho, vp, vs), a point source at the
+    box centre, depth_m below one surface receiver, with a Gaussian source time function
+    exp(-((t - t0) / sigma)^2) * amplitude. source_type 1/2/3: single force along
+    colatitude / longitude / radius; 10: the moment tensor diag(1, 1, 1) * amplitude."""
+    rng = np.random.default_rng(0)
+    setup = make_setup(n_el, colat=colat, lon=lon, r=r, is_diss=0)
+    box = F.make_boxes(setup)[0]
+    m = build_model(box, rng, is_diss=0)
+    for k, v in {"rhoinv": 1.0 / rho, "mu": rho * vs ** 2, "lambda": rho * (vp ** 2 - 2.0 * vs ** 2)}.items():
+        m[k][:] = np.float32(v)
+    ev = make_event(rng, setup, nt, dt, depth_m, 5.0, 1, jitter_deg=0.0)
+    ev.event.source_type = source_type
+    if source_type == 10:
+        ev.event.mom = np.array([amplitude, amplitude, amplitude, 0.0, 0.0, 0.0], np.float32)
+        amp = 1.0
+    else:
+        amp = amplitude
+    t = np.arange(nt + 1) * float(ev.event.dt)
+    ev.stf = (np.exp(-((t - t0) / sigma) ** 2) * amp).astype(np.float32)
+    ev.receivers.loc[:] = [[float(ev.event.xxs), float(ev.event.yys), 0.0]]
+    relax_tau = np.array([1.7, 17.0, 170.0], np.float32)
+    return Problem(setup, box, relax_tau, np.zeros(3, np.float32), m, [ev], pml=pml, label="homogeneous")
+
+
 def make_problem(name: str, seed: int = 1234, nt: Optional[int] = None, n_el=None, is_diss: int = 1,
                  adjoint_flag: int = 0, n_events: Optional[int] = None, pml: int = 3,
                  n_rec: Optional[int] = None, model: bool = True) -> Problem:

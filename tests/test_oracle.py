@@ -151,3 +151,42 @@ def test_p_wave_travel_time(oracle_mod):
     t_peak = np.argmax(np.abs(uz)) * dt
     expected = 8.0 + 100e3 / 7000.0
     assert abs(t_peak - expected) < 2.0, (t_peak, expected)
+
+
+@pytest.mark.parametrize("source_type,comp,speed", [(1, 0, 4000.0), (2, 1, 4000.0), (3, 2, 7000.0)])
+def test_body_wave_travel_times(oracle_mod, source_type, comp, speed):
+    """Homogeneous elastic box (vp 7 km/s, vs 4 km/s) resolved at the source band: a force
+    150 km below a surface receiver, Gaussian in time (peak at 8 s, sigma 3 s). A horizontal
+    force gives a transverse displacement peaking one S travel time (150 km / vs) after the
+    force peak, a vertical force a vertical displacement peaking one P travel time later."""
+    p = synth.homogeneous_problem(source_type=source_type)
+    o = oracle_mod.Oracle(p, fp64=True)
+    o.run(p.events[0].event.nt)
+    dt = float(p.events[0].event.dt)
+    u = np.cumsum(o.seismograms()[comp][0]) * dt
+    t_peak = np.argmax(np.abs(u)) * dt
+    expected = 8.0 + 150e3 / speed
+    assert abs(t_peak - expected) < 1.5, (t_peak, expected)
+
+
+ENERGY_BOX = dict(n_el=(6, 6, 4), colat=(44.0, 46.0), lon=(9.0, 11.0), r=(6171000.0, 6371000.0), nt=800, dt=0.05,
+                  source_type=10, depth_m=60000.0, t0=3.0, sigma=1.0)
+
+
+def test_energy_conserved_without_pml_and_absorbed_with_pml(oracle_mod, wave_energy):
+    """Elastic homogeneous box, explosion at 60 km depth ending by 6 s. With every boundary
+    traction-free (pml 0) the total energy stays constant to the scheme's fluctuation; with
+    PML on the sides and bottom it never increases and the PML absorbs most of it by 40 s."""
+    series = {}
+    for pml in (0, 2):
+        p = synth.homogeneous_problem(pml=pml, **ENERGY_BOX)
+        o = oracle_mod.Oracle(p, fp64=True)
+        e = []
+        for _ in range(20):                     # t = 2, 4, ..., 40 s
+            o.run(40)
+            e.append(wave_energy(o.get, o.get, p))
+        series[pml] = np.array(e)
+    free, absorbed = series[0][3:], series[2][4:]      # t >= 8 s, t >= 10 s
+    assert free.max() - free.min() < 0.03 * free.mean(), free
+    assert np.all(absorbed[1:] <= 1.005 * absorbed[:-1]), absorbed
+    assert absorbed[-1] < 0.35 * series[2][3], (absorbed[-1], series[2][3])
