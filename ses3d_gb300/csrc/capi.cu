@@ -548,6 +548,8 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
       c.a_k[k] = cfg->dt / cfg->tau_p[k];
       c.L_k[k] = cfg->dt * cfg->D_p[k] / cfg->tau_p[k];
     }
+    const float dPdalpha[3] = {-3.06f, -1.54f, 2.56f};  // ses3d_grad_Q.f90:30-32
+    c.q_alpha_w[k] = cfg->D_p[k] != 0.f ? dPdalpha[k] * cfg->tau_p[k] / cfg->D_p[k] : 0.f;
   }
   c.s_grad = (float)cfg->samp_ad * cfg->dt;
   c.pml = cfg->pml;
@@ -560,7 +562,7 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
     c.gx_shift = l - 1;
   }
   c.Jac = g.Jac;
-  c.inv_jac = 1.f / g.Jac;
+  c.s_jac = (double)c.s_grad / (double)g.Jac;
   // coefficient tables
   KTab kt;
   for (int i = 0; i < NP; ++i)

@@ -235,7 +235,7 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
                          2.f * exz_ad * exzf + 2.f * eyz_ad * eyzf;
       const float *GM = p.gmat + m0;
       const float rho = GM[G_RHO * N], cp = GM[G_CP * N], cs = GM[G_CS * N];
-      const double sj = (double)c.s_grad / (double)c.Jac;
+      const double sj = c.s_jac;
       double *GR = p.grad + (size_t)ev * NGRAD * N + m0;
       GR[0 * N] += sj * (double)((vxf * vx + vyf * vy + vzf * vz) +
                                  ((cp * cp - 2.f * cs * cs) * tr_fw * tr_ad + 2.f * cs * cs * edde));
@@ -243,9 +243,10 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
       GR[2 * N] += sj * (double)(4.f * rho * cs * (edde - tr_ad * tr_fw - 2.f * exzf * exz_ad - 2.f * eyzf * eyz_ad));
       GR[3 * N] += sj * (double)(8.f * rho * cs * (exzf * exz_ad + eyzf * eyz_ad));
       if (DISS && p.grad_q) {
-        const float dPdalpha[3] = {-3.06f, -1.54f, 2.56f};
+        // The three mechanisms' terms are summed in FP32 and the sum accumulated in FP64:
+        // one conversion and one FMA per kernel (FP64 issue is scarce on this part).
         const float ef[6] = {exxf, eyyf, ezzf, exyf, exzf, eyzf};
-        double gq = 0.0, ga = 0.0, gk = 0.0, gak = 0.0;
+        float gq = 0.f, ga = 0.f, gk = 0.f, gak = 0.f;
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
           const float tsum = Mv[m] + Mv[3 + m] + Mv[6 + m];
@@ -253,16 +254,16 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
 #pragma unroll
           for (int cc = 0; cc < 6; ++cc) Md += Mv[3 * cc + m] * ef[cc];
           Md = Md - tr_fw * tsum / 3.f;
-          gq += (double)(Md * c.tau_p[m]);
-          ga += (double)(Md * dPdalpha[m] * c.tau_p[m] / c.D_p[m]);
+          gq += Md * c.tau_p[m];
+          ga += Md * c.q_alpha_w[m];
           const float Mk = tsum * tr_fw;
-          gk += (double)(Mk * c.tau_p[m]);
-          gak += (double)(Mk * dPdalpha[m] * c.tau_p[m] / c.D_p[m]);
+          gk += Mk * c.tau_p[m];
+          gak += Mk * c.q_alpha_w[m];
         }
-        GR[4 * N] += sj * gq;
-        GR[5 * N] += sj * ga;
-        GR[6 * N] += sj * gk;
-        GR[7 * N] += sj * gak;
+        GR[4 * N] += sj * (double)gq;
+        GR[5 * N] += sj * (double)ga;
+        GR[6 * N] += sj * (double)gk;
+        GR[7 * N] += sj * (double)gak;
       }
     }
   }

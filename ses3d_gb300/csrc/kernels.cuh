@@ -48,15 +48,16 @@ struct Consts {
   float a_k[3];   // dt / tau_p(k)
   float L_k[3];   // dt * D_p(k) / tau_p(k)
   float s_grad;   // samp_ad * dt
-  float inv_jac;  // unused by the reference-order path; kept for the Q kernels
   float Jac;
   float tau_p[3], D_p[3];
+  float q_alpha_w[3];  // dP/dalpha_k tau_k / D_k of the alpha kernels (ses3d_grad_Q.f90:126)
   int pml;        // PML width in elements
   int lean;       // plain forward: displacement gradients kept only in PML elements
   // t / GX for 32-bit t as (m + ((t - m) >> 1)) >> shift with m = umulhi(t, gx_magic)
   // (division by an invariant integer, Granlund & Montgomery 1994); GX >= 2
   unsigned gx_magic;
   int gx_shift;
+  double s_jac;   // samp_ad dt / Jac in FP64: the weight of one kernel-correlation term
 };
 
 struct Ptrs {
