@@ -892,6 +892,7 @@ static int state_field_index(int field) {
 static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float *hin) {
   int rc = check_event(h, event);
   if (rc) return rc;
+  if (field < 0 || field >= SES3D_FIELD_COUNT) return fail(h, SES3D_E_CONFIG, "unknown field");
   const long long N = h->geo.N, G = h->geo.G;
   float *vbase = h->d_v + (size_t)event * 3 * G;
   float *sbase = h->d_state + (size_t)event * NSTATE * N;
@@ -899,7 +900,6 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
     float *d = vbase + (size_t)(field - SES3D_FIELD_VX_GLOBAL) * G;
     if (hout) CK(h, cudaMemcpy(hout, d, G * sizeof(float), cudaMemcpyDeviceToHost));
     else CK(h, cudaMemcpy(d, hin, G * sizeof(float), cudaMemcpyHostToDevice));
-    destroy_graph(h);
     return SES3D_OK;
   }
   if (field == SES3D_FIELD_MM_GLOBAL) {
@@ -910,7 +910,6 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
   float *tmp = nullptr, *tmp2 = nullptr;
   CK(h, dalloc(&tmp, (size_t)N));
   CK(h, dalloc(&tmp2, (size_t)N));
-  int out_rc = SES3D_OK;
   auto done = [&](int r) { dfree(tmp); dfree(tmp2); return r; };
   if (field >= SES3D_FIELD_VX && field <= SES3D_FIELD_VZ) {
     if (!hout) return done(fail(h, SES3D_E_CONFIG, "local v is derived from the global v; set the global field"));
@@ -951,13 +950,10 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
         if (e != cudaSuccess) return done(cuda_fail(h, e, "memory variable transfer"));
       }
     }
-  } else {
-    out_rc = fail(h, SES3D_E_CONFIG, "unknown field");
   }
   cudaError_t e = cudaStreamSynchronize(h->st);
   if (e != cudaSuccess) return done(cuda_fail(h, e, "field sync"));
-  destroy_graph(h);
-  return done(out_rc);
+  return done(SES3D_OK);
 }
 
 int ses3d_gpu_get_field(ses3d_gpu *h, int event, int field, float *out) {

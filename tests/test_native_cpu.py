@@ -93,3 +93,32 @@ def test_fortran_interface_block_covers_header():
             "const char *": "type(c_ptr)", "void *": "type(c_ptr)"}
     for name, ret in decl.items():
         assert fort[name] == want[ret], (name, ret, fort[name])
+
+
+@pytest.mark.parametrize("field,value,fragment", [("nt", 0, b"nt"), ("dt", 0.0, b"dt"), ("adjoint_flag", 3, b"adjoint_flag"),
+                                                  ("is_diss", 2, b"is_diss"), ("n_events", 0, b"n_events")])
+def test_create_validates_before_touching_a_device(native, field, value, fragment):
+    """Configuration errors are reported before any device call (so also without a GPU)."""
+    from ses3d_gb300 import _lib
+    from ses3d_gb300 import synth
+    from ses3d_gb300.solver import config_from
+    p = synth.make_problem("tiny", nt=5, model=False)
+    cfg = config_from(p.box, p.setup, 5, p.events[0].event.dt, p.tau, p.D, pml=3)
+    setattr(cfg, field, value)
+    h = ctypes.c_void_p()
+    assert native.ses3d_gpu_create(ctypes.byref(cfg), ctypes.byref(h)) == -1
+    assert fragment in native.ses3d_gpu_last_error(None)
+
+
+def test_misfit_gradient_validates_arguments(native):
+    from ses3d_gb300 import _lib
+    from ses3d_gb300 import synth
+    from ses3d_gb300.solver import config_from
+    p = synth.make_problem("tiny", nt=5, model=False)
+    cfg = config_from(p.box, p.setup, 5, p.events[0].event.dt, p.tau, p.D, pml=3)
+    dummy = ctypes.c_void_p(16)  # never dereferenced: the checks fail first
+    assert native.ses3d_gpu_misfit_gradient_device(ctypes.byref(cfg), None, 1.0, None, dummy, 0) == -1
+    assert b"null" in native.ses3d_gpu_last_error(None)
+    cfg.lpd = 5
+    assert native.ses3d_gpu_misfit_gradient_device(ctypes.byref(cfg), dummy, 1.0, None, dummy, 0) == -1
+    assert b"lpd" in native.ses3d_gpu_last_error(None)
