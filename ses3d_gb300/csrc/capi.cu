@@ -111,7 +111,9 @@ struct ses3d_gpu {
   std::vector<int> rec_off;  // [nev+1]
   double *d_grad = nullptr;
   unsigned int *d_scratch_u = nullptr;
-  std::vector<float *> records;  // each [nev][NREC][N]
+  std::vector<float *> records;  // each [nev][NREC][N], inside record_blocks
+  std::vector<float *> record_blocks;  // owned allocations holding the records
+  std::vector<float *> record_slots;   // preallocated record places of a flag-1 run
   int record_cursor = 0;
   std::vector<int> store_steps;   // iterations whose forward fields are stored (1-based)
   int nrec_done = 0;              // records produced by the forward run so far
@@ -659,7 +661,7 @@ int ses3d_gpu_destroy(ses3d_gpu *h) {
   for (void *p : ptrs) dfree(p);
   free_forces(h->fset[0]);
   free_forces(h->fset[1]);
-  for (float *r : h->records) dfree(r);
+  for (float *r : h->record_blocks) dfree(r);
   for (float *r : h->ckpts) dfree(r);
   for (float *r : h->segbuf) dfree(r);
   if (h->st) cudaStreamDestroy(h->st);
@@ -829,7 +831,20 @@ int ses3d_gpu_step(ses3d_gpu *h, int n) {
           if (rc) return rc;
         }
       } else {
-        CK(h, dalloc(&rec, (size_t)h->cfg.n_events * NREC * h->geo.N));
+        const size_t rec_floats = (size_t)h->cfg.n_events * NREC * h->geo.N;
+        if (h->records.empty()) {  // one allocation for every record of the run
+          const size_t n = std::max<size_t>(1, h->store_steps.size());
+          float *block = nullptr;
+          CK(h, dalloc(&block, n * rec_floats));
+          h->record_blocks.push_back(block);
+          for (size_t r = 0; r < n; ++r) h->record_slots.push_back(block + r * rec_floats);
+        }
+        if (h->records.size() < h->record_slots.size()) {
+          rec = h->record_slots[h->records.size()];
+        } else {
+          CK(h, dalloc(&rec, rec_floats));
+          h->record_blocks.push_back(rec);
+        }
         h->records.push_back(rec);
         mode = 1;
       }
@@ -1082,6 +1097,7 @@ int ses3d_gpu_put_record(ses3d_gpu *h, int event, int record, const float *in) {
   if (record == (int)h->records.size()) {
     float *r = nullptr;
     CK(h, dalloc(&r, (size_t)h->cfg.n_events * NREC * N));
+    h->record_blocks.push_back(r);
     CK(h, cudaMemset(r, 0, (size_t)h->cfg.n_events * NREC * N * sizeof(float)));
     h->records.push_back(r);
     h->record_cursor = (int)h->records.size();
@@ -1276,7 +1292,7 @@ int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
              nev * ((size_t)NSTATE * N + 6 * G);
   size_t bytes = f * sizeof(float);
   if (h->d_grad) bytes += nev * NGRAD * N * sizeof(double);
-  bytes += h->records.size() * nev * NREC * N * sizeof(float);
+  bytes += std::max(h->records.size(), h->record_slots.size()) * nev * NREC * N * sizeof(float);
   bytes += h->ckpts.size() * ckpt_floats(h) * sizeof(float);
   bytes += h->segbuf.size() * nev * NREC * N * sizeof(float);
   if (h->d_state2) bytes += nev * ((size_t)NSTATE * N + 3 * G) * sizeof(float);
