@@ -109,6 +109,27 @@ def test_c1_configuration_prefix(native, oracle_mod):
         assert rel(g[c], r[c]) <= SEIS_TOL_FP32, (c, rel(g[c], r[c]))
 
 
+def test_c1_configuration_full_length(native, oracle_mod):
+    """The small plain-forward workload at its full length (22 x 22 x 10 elements, nt = 1000,
+    10 receivers): seismograms within 1e-5 of the FP32 oracle and 1e-4 of the FP64 oracle."""
+    from ses3d_gb300.solver import Simulation
+    p = synth.make_problem("c1")
+    nt = p.events[0].event.nt
+    assert nt == 1000
+    with Simulation.from_problem(p) as sim:
+        sim.use_graph(True, 10)
+        sim.set_lean(True)
+        sim.run()
+        g = sim.seismograms(0)
+    for fp64, tol in ((False, SEIS_TOL_FP32), (True, SEIS_TOL_FP64)):
+        o = oracle_mod.Oracle(p, fp64=fp64)
+        o.run(nt)
+        r = o.seismograms()
+        for c in range(3):
+            assert np.abs(r[c]).max() > 0
+            assert rel(g[c], r[c]) <= tol, (fp64, c, rel(g[c], r[c]))
+
+
 @pytest.mark.parametrize("is_diss,source_type", [(0, 10), (0, 1), (1, 2), (0, 3)])
 def test_variants(native, oracle_mod, is_diss, source_type):
     from ses3d_gb300.solver import Simulation
