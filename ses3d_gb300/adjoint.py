@@ -134,6 +134,7 @@ class MisfitSetup:
         """Forward run of the given events (default: all) on the model records (device
         tensors). adjoint: keep the forward records, or checkpoints every K records."""
         evs = list(range(len(self.events))) if events is None else list(events)
+        self.check_records(records)
         sim = Simulation(self._config(1 if adjoint else 0, len(evs)))
         sim.set_model_device([records[k].data_ptr() if k in records else 0 for k in
                               ("rhoinv", "mu", "lambda", "A", "B", "C", "Q")])
@@ -149,6 +150,23 @@ class MisfitSetup:
             self.last["records_per_segment"] = K
         sim.run()
         return sim
+
+    @property
+    def n_points(self) -> int:
+        """GLL points of the mesh (the length of every model record)."""
+        c = self.cfg_template
+        return 125 * (c.nx + 1) * (c.ny + 1) * (c.nz + 1)
+
+    def check_records(self, records: dict):
+        """Model records must be contiguous FP32 CUDA tensors of n_points values: the library
+        reads them through raw device pointers."""
+        import torch
+        for k, t in records.items():
+            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()):
+                raise TypeError("model record %s must be a contiguous float32 CUDA tensor" % k)
+            if t.numel() != self.n_points:
+                raise ValueError("model record %s holds %d values; the mesh has %d GLL points"
+                                 % (k, t.numel(), self.n_points))
 
     # -- memory plan ---------------------------------------------------------------------------
     def budget(self) -> float:
@@ -284,6 +302,10 @@ def misfit_gradients_device(cfg: L.Config, ksum: list, grad_out: float, Q) -> li
     import torch
     if Q.dtype not in (torch.float32, torch.float64):
         raise TypeError("model tensors must be float32 or float64")
+    n = 125 * (cfg.nx + 1) * (cfg.ny + 1) * (cfg.nz + 1)
+    if not Q.is_cuda or Q.numel() != n or any(k.numel() != n or k.dtype != torch.float64 or not k.is_cuda
+                                               or not k.is_contiguous() for k in ksum):
+        raise ValueError("kernels and Q must be CUDA tensors of %d values (kernels contiguous float64)" % n)
     lib = L.load()
     f64 = int(Q.dtype == torch.float64)
     q = Q.detach().contiguous()

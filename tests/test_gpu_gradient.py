@@ -116,3 +116,23 @@ def test_sub_batched_gradient_equals_one_batch(native, per_batch, ckpt):
             assert np.array_equal(a, b)              # same FP64 summation order
         else:
             assert np.allclose(a, b, rtol=1e-12, atol=0)
+
+
+def test_wrong_sized_model_tensors_are_rejected_before_any_device_work(native):
+    """The library reads model records and kernels through raw device pointers, so the
+    Python side checks their sizes and types first."""
+    import torch
+    from ses3d_gb300 import adjoint as A
+    p = synth.make_problem("tiny", nt=20, seed=43, adjoint_flag=1)
+    setup = A.MisfitSetup.from_problem(p, samp_ad=5)
+    m = list(A.problem_tensors(p))
+    short = [t[:-1].contiguous() for t in m]
+    with pytest.raises(ValueError, match="GLL points"):
+        A.waveform_misfit(setup, *short)
+    with pytest.raises(TypeError, match="CUDA"):
+        setup.simulate({"rhoinv": torch.ones(setup.n_points)})
+    ksum = [torch.zeros(setup.n_points, dtype=torch.float64, device="cuda") for _ in range(5)]
+    with pytest.raises(ValueError, match="CUDA tensors"):
+        A.misfit_gradients_device(setup.cfg_template, ksum[:4] + [ksum[4][:-1]], 1.0, m[4])
+    g = A.misfit_gradients_device(setup.cfg_template, ksum, 1.0, m[4])
+    assert all(t.shape == m[4].shape and torch.all(t == 0) for t in g)
