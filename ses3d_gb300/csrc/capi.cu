@@ -154,7 +154,10 @@ int fail(ses3d_gpu *h, int code, const std::string &msg) {
 
 int cuda_fail(ses3d_gpu *h, cudaError_t e, const char *where) {
   std::string m = std::string(where) + ": " + cudaGetErrorString(e);
-  return fail(h, SES3D_E_CUDA, m);
+  // a failed allocation also sets the runtime's last error; clear it so that the next
+  // launch check (cudaGetLastError) does not report it again
+  cudaGetLastError();
+  return fail(h, e == cudaErrorMemoryAllocation ? SES3D_E_OOM : SES3D_E_CUDA, m);
 }
 
 #define CK(h, call)                                              \
@@ -617,6 +620,7 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   if (cfg->adjoint_flag == 2) chk(dalloc(&h->d_grad, nev * NGRAD * g.N));
   if (e != cudaSuccess) {
     std::string m = std::string("allocation: ") + cudaGetErrorString(e);
+    cudaGetLastError();  // clear the failed allocation's last error
     ses3d_gpu_destroy(h);
     return fail(nullptr, e == cudaErrorMemoryAllocation ? SES3D_E_OOM : SES3D_E_CUDA, m);
   }

@@ -92,3 +92,20 @@ def test_adjoint_handle_rejections(native):
                                             ctypes.c_void_p(v.data_ptr()), 1)
         assert rc == CONFIG and b"16-byte" in native.ses3d_gpu_last_error(sim.h)
         assert sim.it == 0
+
+
+def test_out_of_memory_is_reported_and_leaves_the_library_usable(native):
+    """A handle whose element state cannot fit (64 events on the 96 x 96 x 40 mesh, 424 GB)
+    fails with SES3D_E_OOM and frees what it had allocated; a following handle steps and
+    its launches are not blamed for the failed allocation."""
+    from ses3d_gb300 import _lib
+    from ses3d_gb300.solver import Simulation, config_from
+    p = synth.make_problem("c2", nt=5, seed=63, model=False, n_events=1)
+    cfg = config_from(p.box, p.setup, 5, p.events[0].event.dt, p.tau, p.D, pml=p.pml, n_events=64)
+    with pytest.raises(_lib.Ses3dError) as ei:
+        Simulation(cfg)
+    assert ei.value.code == -2 and "allocation" in str(ei.value)
+    q = synth.make_problem("tiny", nt=10, seed=64)
+    with Simulation.from_problem(q) as sim:
+        sim.run()
+        assert np.abs(np.concatenate(sim.seismograms(0))).max() > 0
