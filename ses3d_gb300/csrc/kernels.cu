@@ -17,7 +17,10 @@
 #ifndef SES3D_ELEM_MINB
 #define SES3D_ELEM_MINB 6
 #endif
-// The same for k_node (256-thread CTAs).
+// Threads per k_node CTA and the minimum resident CTAs per SM requested from ptxas.
+#ifndef SES3D_NODE_TPB
+#define SES3D_NODE_TPB 256
+#endif
 #ifndef SES3D_NODE_MINB
 #define SES3D_NODE_MINB 7
 #endif
@@ -654,17 +657,17 @@ __global__ void __launch_bounds__(TPE, SES3D_TMA_MINB) k_element_tma(const Const
 }
 
 // ---------------------------------------------------------------------------------------
-// k_node: one thread per (global node, event); grid (ceil(GX*GY/256), GZ, n_events).
+// k_node: one thread per (global node, event); grid (ceil(GX*GY/TPB), GZ, n_events).
 // Deterministic assembly in the reference order (element i, then j, then k ascending;
 // ses3d_evolution.f90:286-310), then a = s / MM, v += dt (a - prof v), v *= taper
 // (ses3d_evolution.f90:318-328,366).
 // ---------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, SES3D_NODE_MINB) k_node(const Consts c, const Ptrs p) {
+__global__ void __launch_bounds__(SES3D_NODE_TPB, SES3D_NODE_MINB) k_node(const Consts c, const Ptrs p) {
   const int gz = blockIdx.y, ev = blockIdx.z;
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
     *p.d_it += 1;  // every reader of the counter ran earlier in stream order
   const unsigned GXY = (unsigned)c.GX * (unsigned)c.GY;
-  const unsigned t = blockIdx.x * 256u + threadIdx.x;
+  const unsigned t = blockIdx.x * (unsigned)SES3D_NODE_TPB + threadIdx.x;
   if (t >= GXY) return;
 #if SES3D_NODE_MAGIC
   const unsigned hi = __umulhi(t, c.gx_magic);
@@ -1108,8 +1111,8 @@ cudaError_t launch_element(int diss, int mode, int epb, const Consts &c, const P
 }
 
 cudaError_t launch_node(const Consts &c, const Ptrs &p, cudaStream_t st) {
-  dim3 grid((unsigned)(((long long)c.GX * c.GY + 255) / 256), (unsigned)c.GZ, (unsigned)c.nev);
-  k_node<<<grid, 256, 0, st>>>(c, p);
+  dim3 grid((unsigned)(((long long)c.GX * c.GY + SES3D_NODE_TPB - 1) / SES3D_NODE_TPB), (unsigned)c.GZ, (unsigned)c.nev);
+  k_node<<<grid, SES3D_NODE_TPB, 0, st>>>(c, p);
   return cudaGetLastError();
 }
 
