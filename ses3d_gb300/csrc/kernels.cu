@@ -111,41 +111,49 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
     eyz = -vy * ir + eyz * irs;
     exy = exy * ir;
     eyx = -vy * ct * ir + eyx * irs;
-    // displacement gradients (ses3d_evolution.f90:109-117)
     const float dt = c.dt;
-    const float dxux = sv[F_DXUX] + dt * exx, dyuy = sv[F_DYUY] + dt * eyy, dzuz = sv[F_DZUZ] + dt * ezz;
-    const float dxuy = sv[F_DXUY] + dt * exy, dyux = sv[F_DYUX] + dt * eyx;
-    const float dxuz = sv[F_DXUZ] + dt * exz, dzux = sv[F_DZUX] + dt * ezx;
-    const float dyuz = sv[F_DYUZ] + dt * eyz, dzuy = sv[F_DZUY] + dt * ezy;
-    if (full) {
-      S[F_DXUX * 125] = dxux; S[F_DYUY * 125] = dyuy; S[F_DZUZ * 125] = dzuz;
-      S[F_DXUY * 125] = dxuy; S[F_DYUX * 125] = dyux; S[F_DXUZ * 125] = dxuz;
-      S[F_DZUX * 125] = dzux; S[F_DYUZ * 125] = dyuz; S[F_DZUY * 125] = dzuy;
-    }
-    // PML profiles of this node (ses3d_init.f90:678-686), corners normalised
-    const float pxr = lt ? lt[LT_PX + in] : __ldg(p.pxr + ii * 5 + in);
-    const float pyr = lt ? lt[LT_PY + jn] : __ldg(p.pyr + j * 5 + jn);
-    const float pzr = lt ? lt[LT_PZ + kn] : __ldg(p.pzr + k * 5 + kn);
+    // Lean iterations in elements outside the PML: every profile there is zero and the taper
+    // one, so the displacement gradients enter nothing and the PML strain terms add zeros;
+    // both are skipped (the strain rates keep their values).
+    const bool pml_free = MODE == 3 && !full;
+    float dxux = 0.f, dyuy = 0.f, dzuz = 0.f, dxuy = 0.f, dyux = 0.f, dxuz = 0.f, dzux = 0.f, dyuz = 0.f, dzuy = 0.f;
     float px = 0.f, py = 0.f, pz = 0.f, taper = 1.f;
-    const float praw = __fadd_rn(__fadd_rn(pxr, pyr), pzr);
-    if (praw != 0.f) {
-      const float den = __fadd_rn(1.f, __fdiv_rn(praw, 1.2f));
-      pz = __fdiv_rn(__fmul_rn(2.f, pzr), den);
-      py = __fdiv_rn(__fmul_rn(2.f, pyr), den);
-      px = __fdiv_rn(__fmul_rn(2.f, pxr), den);
-      const float prof = __fadd_rn(__fadd_rn(px, py), pz);
-      taper = expf(-__fmul_rn(__fmul_rn(0.1f, prof), prof));
+    if (!pml_free) {
+      // displacement gradients (ses3d_evolution.f90:109-117)
+      dxux = sv[F_DXUX] + dt * exx; dyuy = sv[F_DYUY] + dt * eyy; dzuz = sv[F_DZUZ] + dt * ezz;
+      dxuy = sv[F_DXUY] + dt * exy; dyux = sv[F_DYUX] + dt * eyx;
+      dxuz = sv[F_DXUZ] + dt * exz; dzux = sv[F_DZUX] + dt * ezx;
+      dyuz = sv[F_DYUZ] + dt * eyz; dzuy = sv[F_DZUY] + dt * ezy;
+      if (full) {
+        S[F_DXUX * 125] = dxux; S[F_DYUY * 125] = dyuy; S[F_DZUZ * 125] = dzuz;
+        S[F_DXUY * 125] = dxuy; S[F_DYUX * 125] = dyux; S[F_DXUZ * 125] = dxuz;
+        S[F_DZUX * 125] = dzux; S[F_DYUZ * 125] = dyuz; S[F_DZUY * 125] = dzuy;
+      }
+      // PML profiles of this node (ses3d_init.f90:678-686), corners normalised
+      const float pxr = lt ? lt[LT_PX + in] : __ldg(p.pxr + ii * 5 + in);
+      const float pyr = lt ? lt[LT_PY + jn] : __ldg(p.pyr + j * 5 + jn);
+      const float pzr = lt ? lt[LT_PZ + kn] : __ldg(p.pzr + k * 5 + kn);
+      const float praw = __fadd_rn(__fadd_rn(pxr, pyr), pzr);
+      if (praw != 0.f) {
+        const float den = __fadd_rn(1.f, __fdiv_rn(praw, 1.2f));
+        pz = __fdiv_rn(__fmul_rn(2.f, pzr), den);
+        py = __fdiv_rn(__fmul_rn(2.f, pyr), den);
+        px = __fdiv_rn(__fmul_rn(2.f, pxr), den);
+        const float prof = __fadd_rn(__fadd_rn(px, py), pz);
+        taper = expf(-__fmul_rn(__fmul_rn(0.1f, prof), prof));
+      }
+      // PML strain rates (ses3d_evolution.f90:123-134)
+      exx = exx + (pz + py) * dxux;
+      eyy = eyy + (px + pz) * dyuy;
+      ezz = ezz + (px + py) * dzuz;
+      exy = exy + (py + pz) * dxuy;
+      eyx = eyx + (px + pz) * dyux;
+      exz = exz + (py + pz) * dxuz;
+      ezx = ezx + (px + py) * dzux;
+      eyz = eyz + (px + pz) * dyuz;
+      ezy = ezy + (px + py) * dzuy;
     }
-    // PML strain rates and symmetrisation (ses3d_evolution.f90:123-138)
-    exx = exx + (pz + py) * dxux;
-    eyy = eyy + (px + pz) * dyuy;
-    ezz = ezz + (px + py) * dzuz;
-    exy = exy + (py + pz) * dxuy;
-    eyx = eyx + (px + pz) * dyux;
-    exz = exz + (py + pz) * dxuz;
-    ezx = ezx + (px + py) * dzux;
-    eyz = eyz + (px + pz) * dyuz;
-    ezy = ezy + (px + py) * dzuy;
+    // symmetrisation (ses3d_evolution.f90:136-138)
     exy = (exy + eyx) * 0.5f;
     exz = (exz + ezx) * 0.5f;
     eyz = (eyz + ezy) * 0.5f;
@@ -189,15 +197,25 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
     float s_xx = sv[F_SXX], s_yy = sv[F_SYY], s_zz = sv[F_SZZ];
     float s_xy = sv[F_SXY], s_yx = sv[F_SYX], s_xz = sv[F_SXZ];
     float s_zx = sv[F_SZX], s_yz = sv[F_SYZ], s_zy = sv[F_SZY];
-    s_xx = s_xx + dt * (sxx - px * s_xx);
-    s_yy = s_yy + dt * (syy - py * s_yy);
-    s_zz = s_zz + dt * (szz - pz * s_zz);
-    s_xy = s_xy + dt * (sxy - px * s_xy);
-    s_yx = s_yx + dt * (sxy - py * s_yx);
-    s_xz = s_xz + dt * (sxz - px * s_xz);
-    s_zx = s_zx + dt * (sxz - pz * s_zx);
-    s_yz = s_yz + dt * (syz - py * s_yz);
-    s_zy = s_zy + dt * (syz - pz * s_zy);
+    if (pml_free) {  // zero profiles; the mirrors equal their partners (lean stepping)
+      s_xx = s_xx + dt * sxx;
+      s_yy = s_yy + dt * syy;
+      s_zz = s_zz + dt * szz;
+      s_xy = s_xy + dt * sxy;
+      s_xz = s_xz + dt * sxz;
+      s_yz = s_yz + dt * syz;
+      s_yx = s_xy; s_zx = s_xz; s_zy = s_yz;
+    } else {
+      s_xx = s_xx + dt * (sxx - px * s_xx);
+      s_yy = s_yy + dt * (syy - py * s_yy);
+      s_zz = s_zz + dt * (szz - pz * s_zz);
+      s_xy = s_xy + dt * (sxy - px * s_xy);
+      s_yx = s_yx + dt * (sxy - py * s_yx);
+      s_xz = s_xz + dt * (sxz - px * s_xz);
+      s_zx = s_zx + dt * (sxz - pz * s_zx);
+      s_yz = s_yz + dt * (syz - py * s_yz);
+      s_zy = s_zy + dt * (syz - pz * s_zy);
+    }
     // taper (ses3d_evolution.f90:368-371); the divergence below uses the untapered values
     S[F_SXX * 125] = s_xx * taper; S[F_SYY * 125] = s_yy * taper; S[F_SZZ * 125] = s_zz * taper;
     S[F_SXY * 125] = s_xy * taper; S[F_SXZ * 125] = s_xz * taper; S[F_SYZ * 125] = s_yz * taper;
