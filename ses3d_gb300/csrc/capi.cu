@@ -141,6 +141,7 @@ struct ses3d_gpu {
   // graph
   bool graph_on = false;
   int graph_n = 0;
+  int graph_len = 0;  // iterations in the captured graph
   cudaGraphExec_t graph_exec = nullptr;
   bool graph_dirty = true;
 };
@@ -476,13 +477,14 @@ int recompute_segment(ses3d_gpu *h, int s) {
   return SES3D_OK;
 }
 
-int build_graph(ses3d_gpu *h) {
+// Captures `len` plain iterations of the primary wavefield as one CUDA graph.
+int build_graph(ses3d_gpu *h, int len) {
   Range range_("ses3d graph capture");
   destroy_graph(h);
   cudaGraph_t graph;
   CK(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
   long long before = h->launches;
-  for (int s = 0; s < h->graph_n; ++s) {
+  for (int s = 0; s < len; ++s) {
     int rc = launch_iteration(h, primary_wave(h), 0, nullptr);
     if (rc) {
       cudaStreamEndCapture(h->st, &graph);
@@ -496,7 +498,17 @@ int build_graph(ses3d_gpu *h) {
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
   h->graph_dirty = false;
+  h->graph_len = len;
   return SES3D_OK;
+}
+
+// Iteration `it` of a flag-1 run stores a forward record (ses3d_main.f90:144), of a flag-2
+// run correlates one (ses3d_main.f90:168); every other iteration is plain.
+bool special_iteration(const ses3d_gpu *h, int it) {
+  const int nt = h->cfg.nt;
+  if (h->mode_flag == 1) return it % h->cfg.samp_ad == 0 || it == 1 || it == nt;
+  if (h->mode_flag == 2) return h->saving_vector[nt + 1 - it] > 0 && h->record_cursor > 0;
+  return false;
 }
 
 int launches_per_iteration(ses3d_gpu *h) {
@@ -815,16 +827,23 @@ int ses3d_gpu_step(ses3d_gpu *h, int n) {
   while (done < n && h->it < nt) {
     const int it = h->it + 1;
     const int flag = h->mode_flag;
-    if (flag == 0 && h->graph_on && h->graph_n > 0 && n - done >= h->graph_n && nt - h->it >= h->graph_n) {
-      if (h->graph_dirty || !h->graph_exec) {
-        int rc = build_graph(h);
-        if (rc) return rc;
+    // plain iterations replay from a CUDA graph: runs of graph_n in plain forward runs, and
+    // in record / adjoint runs the stretches of samp_ad - 1 between stored iterations
+    const int L = flag == 0 ? h->graph_n : std::min(h->graph_n, h->cfg.samp_ad - 1);
+    if (h->graph_on && L > 0 && n - done >= L && nt - h->it >= L) {
+      bool plain = true;
+      for (int q = 1; flag != 0 && q <= L && plain; ++q) plain = !special_iteration(h, h->it + q);
+      if (plain) {
+        if (h->graph_dirty || !h->graph_exec || h->graph_len != L) {
+          int rc = build_graph(h, L);
+          if (rc) return rc;
+        }
+        CK(h, cudaGraphLaunch(h->graph_exec, h->st));
+        h->launches += (long long)L * launches_per_iteration(h);
+        h->it += L;
+        done += L;
+        continue;
       }
-      CK(h, cudaGraphLaunch(h->graph_exec, h->st));
-      h->launches += (long long)h->graph_n * launches_per_iteration(h);
-      h->it += h->graph_n;
-      done += h->graph_n;
-      continue;
     }
     int mode = 0;
     float *rec = nullptr;

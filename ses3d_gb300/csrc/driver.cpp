@@ -239,6 +239,10 @@ int run_event(const Args &a, const std::string &id) {
     if (api(ses3d_gpu_set_adjoint_sources(h, 0, nad, loc.data(), stf.data(), &nin), h, "set_adjoint_sources") < 0)
       return 1;
   }
+  // plain iterations replay from CUDA graphs; plain forward runs step lean (their outputs,
+  // seismograms and velocity snapshots, do not depend on the displacement gradients)
+  if (api(ses3d_gpu_use_graph(h, 1, 10), h, "use_graph") < 0) return 1;
+  if (cfg.adjoint_flag == 0 && api(ses3d_gpu_set_lean(h, 1), h, "set_lean") < 0) return 1;
   // ---- time loop (SOURCE/ses3d_main.f90:95-178) with ses3d_output every ssamp iterations
   std::vector<float> sx((size_t)nr * cfg.nt), sy(sx.size()), sz(sx.size()), snap(N);
   const float src_deg[3] = {ev.xxs * pi / 180.0f * 180.0f / pi, ev.yys * pi / 180.0f * 180.0f / pi, ev.zzs};

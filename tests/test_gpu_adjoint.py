@@ -203,3 +203,29 @@ def test_device_kernel_sums_and_misfit_gradient(native):
                 assert np.allclose(got, want, rtol=1e-14, atol=0), nm
             else:
                 assert np.allclose(got, want.astype(np.float32), rtol=1e-6, atol=0), nm
+
+
+@pytest.mark.parametrize("K", [0, 3])
+def test_graph_replay_in_record_and_adjoint_runs(native, problem, runs, K):
+    """Flag-1 and flag-2 runs replaying their plain stretches from CUDA graphs store the same
+    records and give the same seismograms and kernels as eager runs, with records kept or
+    checkpointed."""
+    from ses3d_gb300 import _lib
+    from ses3d_gb300.solver import Simulation
+    p = problem
+    with Simulation.from_problem(p, adjoint_flag=1, grad_variant=1) as sim:
+        sim.use_graph(True, 10)
+        if K:
+            _lib.check(sim.lib.ses3d_gpu_set_checkpointing(sim.h, K), sim.h)
+        before = sim.launch_count
+        sim.run()
+        assert sim.launch_count - before > 0
+        if not K:
+            for r in range(sim.record_count()):
+                assert np.array_equal(sim.record(r), runs["gpu_records"][r]), r
+        loc, stf = adjoint_inputs(p, sim.seismograms(0))
+        sim.set_adjoint_sources(0, loc, stf)
+        sim.begin_adjoint()
+        sim.run()
+        for k in ("rho", "cp", "csh", "csv", "Q_mu"):
+            assert np.array_equal(sim.kernel(k), runs["gpu_kernels"][k]), k
