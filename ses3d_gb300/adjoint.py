@@ -143,6 +143,8 @@ class MisfitSetup:
             sim.set_source(slot, e.xxs, e.yys, e.zzs, e.source_type, e.mom, e.stf)
             sim.set_receivers(slot, e.recloc)
         sim.use_graph(True, 10)   # plain iterations (between stored ones) replay from CUDA graphs
+        if not adjoint:
+            sim.set_lean(True)        # seismograms only: the displacement gradients enter nothing
         if adjoint:
             if K is None:
                 K = self.plan().K
