@@ -172,6 +172,8 @@ def run_ours(args, rank, world, local):
     if rank == 0 or not os.path.exists(B.LIB):
         B.build()
     barrier(world)
+    from ses3d_gb300.solver import select_device
+    select_device(local if world > 1 else 0)   # the library's runtime follows torch's device
     nt = args.warmup + args.steps + 8  # the block-shape autotune spends 6 of the warm-up steps
     p = synth.make_problem(args.workload, nt=nt, seed=args.seed)
     N = p.n_nodes

@@ -68,6 +68,12 @@ typedef struct {
 /* Library version string. */
 const char *ses3d_gpu_version(void);
 
+/* Makes `device` the current device of this library's CUDA runtime for the calling thread;
+ * handles are created on the current device. A process that drives one GPU of several
+ * (one rank per GPU) selects its GPU before creating handles. No counterpart in the
+ * reference (one MPI rank per core). */
+int ses3d_gpu_select_device(int device);
+
 /* Creates a handle: GLL tables, geometry, PML profiles and all device buffers.
  * Replaces the geometry part of ses3d_init (SOURCE/ses3d_init.f90:87-248,574-709). */
 int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out);

@@ -52,6 +52,7 @@ _lib = None
 
 SIGNATURES = {
     "ses3d_gpu_version": (c_char_p, []),
+    "ses3d_gpu_select_device": (c_int, [c_int]),
     "ses3d_gpu_create": (c_int, [ctypes.POINTER(Config), ctypes.POINTER(c_void_p)]),
     "ses3d_gpu_destroy": (c_int, [c_void_p]),
     "ses3d_gpu_last_error": (c_char_p, [c_void_p]),

@@ -524,6 +524,18 @@ extern "C" {
 
 const char *ses3d_gpu_version(void) { return "ses3d_gb300 0.1 (sm_103a)"; }
 
+int ses3d_gpu_select_device(int device) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return fail(nullptr, SES3D_E_NODEV, "no CUDA device");
+  }
+  if (device < 0 || device >= ndev) return fail(nullptr, SES3D_E_CONFIG, "device index out of range");
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+  return SES3D_OK;
+}
+
 const char *ses3d_gpu_last_error(const ses3d_gpu *h) { return h ? h->err.c_str() : g_create_error.c_str(); }
 
 int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {

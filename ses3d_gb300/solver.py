@@ -41,6 +41,11 @@ def config_from(box: F.Box, setup: F.Setup, nt: int, dt, tau, D, pml: int = 2, a
     return c
 
 
+def select_device(device: int):
+    """Creates later handles of this thread on GPU `device` (one rank per GPU)."""
+    L.check(L.load().ses3d_gpu_select_device(int(device)))
+
+
 class Simulation:
     """One handle of the native library: one mesh, one model, n_events events."""
 

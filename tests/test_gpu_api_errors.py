@@ -109,3 +109,15 @@ def test_out_of_memory_is_reported_and_leaves_the_library_usable(native):
     with Simulation.from_problem(q) as sim:
         sim.run()
         assert np.abs(np.concatenate(sim.seismograms(0))).max() > 0
+
+
+def test_select_device(native):
+    """Device selection for one-rank-per-GPU processes: an index outside the visible devices
+    is refused, the first device is accepted and handles are created on it."""
+    import torch
+    from ses3d_gb300.solver import Simulation, select_device
+    assert native.ses3d_gpu_select_device(torch.cuda.device_count() + 3) == CONFIG
+    assert b"device index" in native.ses3d_gpu_last_error(None)
+    select_device(0)
+    with Simulation.from_problem(synth.make_problem("tiny", nt=5, seed=65)) as sim:
+        sim.run()

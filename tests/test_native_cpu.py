@@ -122,3 +122,11 @@ def test_misfit_gradient_validates_arguments(native):
     cfg.lpd = 5
     assert native.ses3d_gpu_misfit_gradient_device(ctypes.byref(cfg), dummy, 1.0, None, dummy, 0) == -1
     assert b"lpd" in native.ses3d_gpu_last_error(None)
+
+
+def test_select_device_without_gpu_fails_cleanly(native):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    assert native.ses3d_gpu_select_device(0) == -7
+    assert b"no CUDA device" in native.ses3d_gpu_last_error(None)
