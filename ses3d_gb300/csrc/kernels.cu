@@ -1,8 +1,10 @@
 // kernels.cu -- sm_103a kernels of the SES3D time step.
 //
-// One iteration of SOURCE/ses3d_evolution.f90 is three launches:
+// One iteration of SOURCE/ses3d_evolution.f90 is three launches (four with point forces):
 //   k_receivers  record_seismograms on the pre-update velocity (ses3d_output.f90:456-497)
-//   k_element    everything element-local: gather, strain rates, spherical terms,
+//   k_element    everything element-local (k_element_tma: persistent, bulk-copy staged;
+//                k_element: register-staged, record and adjoint iterations): gather,
+//                strain rates, spherical terms,
 //                displacement gradients, PML strain, stress rates, memory variables,
 //                PML stress march, moment source, weak divergence, taper
 //                (ses3d_evolution.f90:27-271,334-360,368-371; ses3d_miscellaneous.f90:97-150)
