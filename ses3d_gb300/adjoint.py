@@ -32,7 +32,7 @@ from typing import List, Optional, Sequence
 import numpy as np
 
 from . import _lib as L
-from .solver import Simulation, config_from
+from .solver import Simulation, config_from, select_device
 
 
 class Bandpass:
@@ -135,6 +135,7 @@ class MisfitSetup:
         tensors). adjoint: keep the forward records, or checkpoints every K records."""
         evs = list(range(len(self.events))) if events is None else list(events)
         self.check_records(records)
+        select_device(next(iter(records.values())).device.index or 0)  # the handle lives with the model
         sim = Simulation(self._config(1 if adjoint else 0, len(evs)))
         sim.set_model_device([records[k].data_ptr() if k in records else 0 for k in
                               ("rhoinv", "mu", "lambda", "A", "B", "C", "Q")])
