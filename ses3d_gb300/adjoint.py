@@ -311,6 +311,7 @@ def misfit_gradients_device(cfg: L.Config, ksum: list, grad_out: float, Q) -> li
                                                or not k.is_contiguous() for k in ksum):
         raise ValueError("kernels and Q must be CUDA tensors of %d values (kernels contiguous float64)" % n)
     lib = L.load()
+    select_device(Q.device.index or 0)
     f64 = int(Q.dtype == torch.float64)
     q = Q.detach().contiguous()
     torch.cuda.synchronize(Q.device)
