@@ -203,6 +203,26 @@ def test_batched_mixed_source_types_match_single(native, lean):
         assert np.array_equal(seis[k], s1[0]) and np.array_equal(vz[k], v1[0]), k
 
 
+@pytest.mark.parametrize("epb", [2, 4])
+def test_lean_register_staged_blocks_bit_identical(native, epb):
+    """Lean stepping in the register-staged element kernel (2 or 4 elements per CTA) on a
+    mesh with elements outside the PML gives the bits of full-state persistent stepping."""
+    from ses3d_gb300.solver import Simulation
+    p = synth.make_problem("small", nt=40, seed=23)
+    outs = []
+    for lean, blocks in ((False, 1), (True, epb)):
+        with Simulation.from_problem(p) as sim:
+            sim.set_lean(lean)
+            sim.set_block_elements(blocks)
+            sim.use_graph(True, 10)
+            sim.run()
+            outs.append((np.concatenate(sim.seismograms(0)), sim.field("vx_global"), sim.field("sxz_pml"),
+                         sim.field("Myz")))
+    assert np.abs(outs[0][0]).max() > 0
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+
+
 def test_graph_and_block_shapes_bit_identical(native):
     from ses3d_gb300.solver import Simulation
     p = synth.make_problem("tiny", nt=40, seed=8)
