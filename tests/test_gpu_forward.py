@@ -130,6 +130,32 @@ def test_c1_configuration_full_length(native, oracle_mod):
             assert rel(g[c], r[c]) <= tol, (fp64, c, rel(g[c], r[c]))
 
 
+@pytest.mark.parametrize("is_diss", [1, 0])
+def test_anisotropic_model_matches_oracle(native, oracle_mod, is_diss):
+    """Nonzero A, B, C (the anisotropic terms of the stress rates, ses3d_evolution.f90:160-200)
+    with seeded point-to-point variation: seismograms and stresses against both oracles."""
+    from ses3d_gb300.solver import Simulation
+    p = synth.make_problem("small", nt=150, seed=27, is_diss=is_diss)
+    rng = np.random.default_rng(27)
+    m = p.model
+    n = m["mu"].size
+    m["A"] = (m["lambda"] * (0.05 + 0.02 * rng.standard_normal(n))).astype(np.float32)
+    m["B"] = (m["mu"] * (0.04 + 0.02 * rng.standard_normal(n))).astype(np.float32)
+    m["C"] = (m["lambda"] * (-0.03 + 0.02 * rng.standard_normal(n))).astype(np.float32)
+    with Simulation.from_problem(p) as sim:
+        sim.run()
+        g = sim.seismograms(0)
+        sxz = sim.field("sxz_pml")
+    for fp64, tol in ((False, SEIS_TOL_FP32), (True, SEIS_TOL_FP64)):
+        o = oracle_mod.Oracle(p, fp64=fp64)
+        o.run(150)
+        r = o.seismograms()
+        for c in range(3):
+            assert np.abs(r[c]).max() > 0
+            assert rel(g[c], r[c]) <= tol, (fp64, c, rel(g[c], r[c]))
+        assert rel(sxz, o.get("sxz_pml")) <= 10 * tol, fp64
+
+
 @pytest.mark.parametrize("is_diss,source_type", [(0, 10), (0, 1), (1, 2), (0, 3)])
 def test_variants(native, oracle_mod, is_diss, source_type):
     from ses3d_gb300.solver import Simulation
