@@ -229,3 +229,32 @@ def test_graph_replay_in_record_and_adjoint_runs(native, problem, runs, K):
         sim.run()
         for k in ("rho", "cp", "csh", "csv", "Q_mu"):
             assert np.array_equal(sim.kernel(k), runs["gpu_kernels"][k]), k
+
+
+def test_elastic_adjoint_kernels_match_oracle(native, oracle_mod):
+    """is_diss = 0 (no memory variables, the elastic element kernels): forward records and
+    the four elastic Frechet kernels against the FP64 oracle."""
+    from ses3d_gb300.solver import Simulation
+    p = synth.make_problem("small", nt=NT, seed=33, adjoint_flag=1, is_diss=0)
+    p.setup.samp_ad = SAMP
+    with Simulation.from_problem(p, adjoint_flag=1) as sim:
+        sim.run()
+        g_rec = [sim.record(r) for r in range(sim.record_count())]
+        loc, stf = adjoint_inputs(p, sim.seismograms(0))
+        sim.set_adjoint_sources(0, loc, stf)
+        sim.begin_adjoint()
+        sim.run()
+        g = {k: sim.kernel(k) for k in ("rho", "cp", "csh", "csv")}
+    o = oracle_mod.Oracle(p, fp64=True, adjoint_flag=1)
+    o.run(NT)
+    recs = np.stack([o.record(r) for r in range(o.nrecords())])
+    assert len(g_rec) == len(recs)
+    assert rel(np.stack(g_rec), recs) <= 1e-4
+    sv = o.get_int("saving_vector")[1:NT + 1]
+    oa = oracle_mod.Oracle(p, fp64=True, adjoint_flag=2, saving_vector=sv, ad_loc=loc, ad_stf=stf)
+    oa.set_records(recs)
+    oa.run(NT)
+    for k in g:
+        ref = oa.get("grad_" + k)
+        assert np.abs(ref).max() > 0, k
+        assert rel(g[k], ref) <= 1e-3, (k, rel(g[k], ref))
