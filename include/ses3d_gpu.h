@@ -39,7 +39,8 @@ extern "C" {
 #define SES3D_E_CUDA (-3)     /* CUDA runtime error */
 #define SES3D_E_STATE (-4)    /* call out of order (e.g. step before set_model) */
 #define SES3D_E_NAN (-5)      /* non-finite wavefield detected by the watchdog */
-#define SES3D_E_NOTFOUND (-6) /* source/receiver outside the box */
+#define SES3D_E_NOTFOUND (-6) /* reserved: a source or receiver outside the box is not an error; it is
+                                 reported through is_source / nr_out, as each reference rank does */
 #define SES3D_E_NODEV (-7)    /* no CUDA device */
 
 typedef struct ses3d_gpu ses3d_gpu;
