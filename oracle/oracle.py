@@ -70,6 +70,7 @@ def load():
         lib.oracle_size.restype = ctypes.c_long
         lib.oracle_size.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
         lib.oracle_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
+        lib.oracle_set.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
         lib.oracle_get_int.restype = ctypes.c_long
         lib.oracle_get_int.argtypes = [ctypes.c_void_p, ctypes.c_char_p, P_i]
         lib.oracle_nrecords.argtypes = [ctypes.c_void_p]
@@ -176,6 +177,15 @@ class Oracle:
         out = np.zeros(n, self.dtype)
         self.lib.oracle_get(self.h, name.encode(), out.ctypes.data_as(ctypes.c_void_p))
         return out
+
+    def set(self, name: str, values) -> None:
+        """Overwrites a named real array (an initial state), converted to the handle's precision."""
+        n = self.lib.oracle_size(self.h, name.encode())
+        a = np.ascontiguousarray(np.asarray(values).reshape(-1), self.dtype)
+        if n < 0 or a.size != n:
+            raise KeyError("%s: %d values for an array of %d" % (name, a.size, n))
+        if self.lib.oracle_set(self.h, name.encode(), a.ctypes.data_as(ctypes.c_void_p)) != 0:
+            raise KeyError(name)
 
     def get_int(self, name: str) -> np.ndarray:
         n = self.lib.oracle_get_int(self.h, name.encode(), None)

@@ -108,6 +108,7 @@ struct Base {
   virtual int nrecords() const = 0;
   virtual int get_record(int r, void *out) = 0;
   virtual int set_records(int nrec, const void *data) = 0;
+  virtual int set(const std::string &name, const void *in) = 0;
 };
 
 template <class T> struct Sim : Base {
@@ -984,6 +985,14 @@ template <class T> struct Sim : Base {
     std::memcpy(out, f->data(), f->size() * sizeof(T));
     return 0;
   }
+  // Overwrites a named state array (initial conditions of parity runs that start from an
+  // arbitrary state rather than at rest); values in the handle's precision.
+  int set(const std::string &nm, const void *in) override {
+    V *f = field(nm);
+    if (!f) return -1;
+    std::memcpy(f->data(), in, f->size() * sizeof(T));
+    return 0;
+  }
   long get_int(const std::string &nm, int *out) override {
     auto put = [&](const std::vector<int> &a) { if (out) std::memcpy(out, a.data(), a.size() * sizeof(int)); return (long)a.size(); };
     auto one = [&](int v) { if (out) out[0] = v; return 1L; };
@@ -1035,6 +1044,7 @@ int oracle_run(void *h, int n) { return static_cast<Base *>(h)->run(n); }
 int oracle_it(void *h) { return static_cast<Base *>(h)->it(); }
 long oracle_size(void *h, const char *name) { return static_cast<Base *>(h)->size(name); }
 int oracle_get(void *h, const char *name, void *out) { return static_cast<Base *>(h)->get(name, out); }
+int oracle_set(void *h, const char *name, const void *in) { return static_cast<Base *>(h)->set(name, in); }
 long oracle_get_int(void *h, const char *name, int *out) { return static_cast<Base *>(h)->get_int(name, out); }
 int oracle_nrecords(void *h) { return static_cast<Base *>(h)->nrecords(); }
 int oracle_get_record(void *h, int r, void *out) { return static_cast<Base *>(h)->get_record(r, out); }

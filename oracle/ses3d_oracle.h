@@ -68,6 +68,9 @@ int   oracle_it(void *h);
 long  oracle_size(void *h, const char *name);
 /* Copies a named real array (float or double, per the handle) into out. */
 int   oracle_get(void *h, const char *name, void *out);
+/* Overwrites a named real array (same names and sizes as oracle_get; values in the
+ * handle's precision): initial states of parity runs. Returns -1 for an unknown name. */
+int   oracle_set(void *h, const char *name, const void *in);
 /* Named integer scalars / arrays (nr, rx, ry, rz, isx, ... ). */
 long  oracle_get_int(void *h, const char *name, int *out);
 /* Forward-field records kept by a flag-1 run (9 fields each, ses3d_main.f90:148-158). */
