@@ -150,7 +150,9 @@ enum {
 
 /* One field of one event in the reference layout (local fields: N = 125(nx+1)(ny+1)(nz+1)
  * floats; memory variables 3N; global fields ((nx+1)*4+1)((ny+1)*4+1)((nz+1)*4+1)).
- * SES3D_FIELD_VX..VZ are the snapshot fields of ses3d_output (SOURCE/ses3d_output.f90:293-312). */
+ * SES3D_FIELD_VX..VZ are the snapshot fields of ses3d_output (SOURCE/ses3d_output.f90:293-312).
+ * SES3D_E_STATE: a displacement gradient after lean iterations (ses3d_gpu_set_lean), or a
+ * handle that steps caller-owned wavefields (ses3d_gpu_step_external). */
 int ses3d_gpu_get_field(ses3d_gpu *h, int event, int field, float *out);
 
 /* Sets one state field (same layout as get_field) -- restart / test injection. */
@@ -281,19 +283,29 @@ int ses3d_gpu_kernel_time(const ses3d_gpu *h, int which, double *total_ms, int64
  *          fields in the order sxx, syy, szz, sxy, sxz, syz, syx, szx, szy (PML
  *          stresses), dxux, dyuy, dzuz, dxuy, dyux, dxuz, dzux, dyuz, dzuy, then the
  *          memory variables Mxx, Myy, Mzz, Mxy, Mxz, Myz with the mechanism fastest
- *          (fields 18-35 unused when is_diss = 0); with lean stepping on, elements
- *          outside the PML keep only the first six stresses and the memory variables
- *          up to date;
+ *          (fields 18-35 unused when is_diss = 0);
  *   v:     n_events x 3 x G floats -- assembled velocity, component-major, global node
  *          gx + GX (gy + GY gz), GX = 4 ex + 1, GY = 4 ey + 1.
  * Zeroed buffers start a run at rest. Model, sources, receivers and the step counter
  * stay in the handle (set up earlier with the calls above); seismograms are recorded
  * into the handle. Only plain forward runs (adjoint_flag 0) are accepted.
+ * Ordering: the library launches on its own stream (ses3d_gpu_stream). The caller's
+ * writes to state and v must be complete before the call (synchronise, or make
+ * ses3d_gpu_stream wait on an event recorded after the writes); the call returns after
+ * its own work on the buffers has finished.
+ * Lean stepping (ses3d_gpu_set_lean) applies: elements outside the PML then keep only the
+ * first six stresses and the memory variables up to date; the displacement gradients
+ * there are not integrated, and the mirror stresses there are brought up to date at the
+ * start of the next call made with lean stepping off.
+ * One handle steps either its own wavefield (ses3d_gpu_step) or caller-owned ones (this
+ * call), not both: after the first external call, ses3d_gpu_step and the wavefield
+ * fields of ses3d_gpu_get_field / set_field return SES3D_E_STATE, and a handle that has
+ * already run ses3d_gpu_step rejects this call with SES3D_E_STATE.
  * The element forces between the element and node kernels live in a fixed array in
  * the library's device memory, 8,388,608 floats (32 MiB), which every GPU that loads
  * the library holds until the process exits: n_events x 3 x N must not exceed it
  * (e.g. one event of at most 2,796,202 GLL points); larger runs get SES3D_E_CONFIG.
- * The first call on a device looks up that array's device address (which may load the
+ * The first call on a handle looks up that array's device address (which may load the
  * library's device code); make it before any stream capture. Calls that overlap on the
  * GPU (two handles or threads stepping at once) share the array and race.
  * The handle's device must be current. No cudaMalloc, cudaFree or other allocating
@@ -307,8 +319,10 @@ int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int n);
  * 96 of the 318 bytes the element kernel moves per GLL point there. Seismograms,
  * velocities, stresses and memory variables are unchanged bit for bit: the mirror
  * stresses are brought up to date before any field transfer and when lean stepping is
- * switched off; SES3D_FIELD_DXUX..DZUY of non-PML elements keep their last values
- * instead of being integrated. begin_adjoint switches lean stepping off. */
+ * switched off. The displacement gradients outside the PML are not integrated, so once a
+ * lean iteration has run, ses3d_gpu_get_field(SES3D_FIELD_DXUX..DZUY) returns
+ * SES3D_E_STATE (for the rest of the run, or until that field is set) instead of values
+ * the reference would not produce. begin_adjoint switches lean stepping off. */
 int ses3d_gpu_set_lean(ses3d_gpu *h, int enable);
 
 /* Element-kernel block shape: elements per CTA (1, 2 or 4); 0 selects the default.

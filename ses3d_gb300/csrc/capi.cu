@@ -101,6 +101,12 @@ struct ses3d_gpu {
   int *d_it = nullptr;
   int *d_err = nullptr;  // device error word (bounded waits)
   bool mirrors_stale = false;  // lean iterations left the mirror stresses outside the PML behind
+  unsigned du_stale = 0;       // bit f: displacement gradient f (dxux..dzuy) not integrated outside the
+                               // PML by lean iterations since the wavefield was last zeroed or set
+  // allocation-free stepping over caller-owned wavefields (ses3d_gpu_step_external)
+  bool external_stepped = false;     // this handle's time axis belongs to an external wavefield
+  bool ext_mirrors_stale = false;    // the last external call stepped lean
+  float *ext_forces = nullptr;       // device address of the fixed element-force array
   int *d_src_elem = nullptr;
   float *d_src_delta = nullptr, *d_src_mom = nullptr, *d_stf = nullptr;
   int *d_src_none = nullptr;  // all -1: no moment source (adjoint iterations)
@@ -342,6 +348,7 @@ int zero_wavefield(ses3d_gpu *h) {
   CK(h, cudaMemsetAsync(h->d_it, 0, sizeof(int), h->st));
   if (h->d_seis) CK(h, cudaMemsetAsync(h->d_seis, 0, (size_t)3 * h->cfg.nt * h->R * sizeof(float), h->st));
   h->mirrors_stale = false;
+  h->du_stale = 0;
   h->it = 0;
   return SES3D_OK;
 }
@@ -834,6 +841,8 @@ int ses3d_gpu_step(ses3d_gpu *h, int n) {
   if (!h) return SES3D_E_CONFIG;
   if (!h->model_set) return fail(h, SES3D_E_STATE, "set_model must be called before step");
   if (n < 0) return fail(h, SES3D_E_CONFIG, "n must be >= 0");
+  if (h->external_stepped)
+    return fail(h, SES3D_E_STATE, "this handle steps a caller-owned wavefield (ses3d_gpu_step_external)");
   const int nt = h->cfg.nt;
   int done = 0;
   while (done < n && h->it < nt) {
@@ -909,7 +918,11 @@ int ses3d_gpu_step(ses3d_gpu *h, int n) {
       ++h->launches;
     }
   }
-  if (done > 0 && h->c.lean) h->mirrors_stale = true;
+  if (done > 0 && h->c.lean) {
+    h->mirrors_stale = true;
+    const Geometry &g = h->geo;  // elements outside the PML exist
+    if (g.ex > 2 * h->cfg.pml && g.ey > 2 * h->cfg.pml && g.ez > h->cfg.pml) h->du_stale = 0x1ffu;
+  }
   CK(h, cudaStreamSynchronize(h->st));
   collect_times(h);
   return check_device_error(h);
@@ -943,6 +956,11 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
   int rc = check_event(h, event);
   if (rc) return rc;
   if (field < 0 || field >= SES3D_FIELD_COUNT) return fail(h, SES3D_E_CONFIG, "unknown field");
+  if (h->external_stepped && field != SES3D_FIELD_MM_GLOBAL)
+    return fail(h, SES3D_E_STATE, "the wavefield of this handle lives in caller-owned buffers (ses3d_gpu_step_external)");
+  if (hout && field >= SES3D_FIELD_DXUX && field <= SES3D_FIELD_DZUY && ((h->du_stale >> (field - SES3D_FIELD_DXUX)) & 1u))
+    return fail(h, SES3D_E_STATE,
+                "lean iterations did not integrate this displacement gradient outside the PML (set_lean)");
   const long long N = h->geo.N, G = h->geo.G;
   float *vbase = h->d_v + (size_t)event * 3 * G;
   float *sbase = h->d_state + (size_t)event * NSTATE * N;
@@ -978,6 +996,8 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
     } else {
       e = cudaMemcpyAsync(tmp, hin, N * sizeof(float), cudaMemcpyHostToDevice, h->st);
       if (e == cudaSuccess) e = launch_state_field(sbase, f, tmp, h->geo.E, 0, h->st);
+      if (e == cudaSuccess && field >= SES3D_FIELD_DXUX && field <= SES3D_FIELD_DZUY)
+        h->du_stale &= ~(1u << (field - SES3D_FIELD_DXUX));
     }
     if (e != cudaSuccess) return done(cuda_fail(h, e, "field transfer"));
   } else if (field >= SES3D_FIELD_MXX && field <= SES3D_FIELD_MYZ) {
@@ -1378,30 +1398,12 @@ int ses3d_gpu_set_block_elements(ses3d_gpu *h, int elements_per_cta) {
 // ---------------------------------------------------------------------------------------
 // Allocation-free iterations over a caller-owned wavefield (ses3d_gpu_step_external).
 // The element forces, scratch between k_element and k_node, live in this fixed array;
-// its device address is looked up once per device and handed to the kernels.
+// each handle looks up its device address on its first external call (the handle was
+// created on that device, after any earlier reset of it) and hands it to the kernels.
 // ---------------------------------------------------------------------------------------
-#include <mutex>
-
 namespace {
 constexpr size_t kStaticForceFloats = (size_t)8 << 20;  // 8,388,608 floats = 32 MiB
 static __device__ __align__(256) float g_static_forces[kStaticForceFloats];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_static_mutex;
-float *g_static_forces_ptr[kMaxDevices] = {nullptr};
-
-// Device address of g_static_forces on the current device (looked up on first use).
-int static_forces(ses3d_gpu *h, int dev, float **out) {
-  std::lock_guard<std::mutex> lock(g_static_mutex);
-  if (!g_static_forces_ptr[dev]) {
-    void *ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_forces);
-    if (e != cudaSuccess || !ptr) return cuda_fail(h, e, "cudaGetSymbolAddress(g_static_forces)");
-    g_static_forces_ptr[dev] = static_cast<float *>(ptr);
-  }
-  *out = g_static_forces_ptr[dev];
-  return SES3D_OK;
-}
 }  // namespace
 
 extern "C" int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int n) {
@@ -1411,6 +1413,8 @@ extern "C" int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int
   if (n < 0) return fail(h, SES3D_E_CONFIG, "n must be >= 0");
   if (!h->model_set) return fail(h, SES3D_E_STATE, "set_model must be called before stepping");
   if (h->mode_flag != 0) return fail(h, SES3D_E_CONFIG, "the external-wavefield step runs plain forward runs only");
+  if (!h->external_stepped && h->it > 0)
+    return fail(h, SES3D_E_STATE, "this handle already stepped its own wavefield (ses3d_gpu_step)");
   const size_t need = (size_t)h->cfg.n_events * 3 * (size_t)h->geo.N;
   if (need > kStaticForceFloats) {
     char msg[256];
@@ -1423,15 +1427,26 @@ extern "C" int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int
   int dev = -1;
   CK(h, cudaGetDevice(&dev));
   if (dev != h->device) return fail(h, SES3D_E_CONFIG, "the handle's device must be current");
-  if (dev < 0 || dev >= kMaxDevices) return fail(h, SES3D_E_CONFIG, "device index out of range");
-  float *forces = nullptr;
-  int rc = static_forces(h, dev, &forces);
-  if (rc) return rc;
+  if (!h->ext_forces) {
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_forces);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGetSymbolAddress(g_static_forces)");
+    if (!ptr) return fail(h, SES3D_E_CUDA, "cudaGetSymbolAddress(g_static_forces) returned no address");
+    h->ext_forces = static_cast<float *>(ptr);
+  }
+  float *forces = h->ext_forces;
+  h->external_stepped = true;
+  if (h->ext_mirrors_stale && !h->c.lean) {  // lean calls left the mirrors outside the PML behind
+    CK(h, launch_sync_mirrors(h->c, state, h->st));
+    ++h->launches;
+    h->ext_mirrors_stale = false;
+  }
   Ptrs p = make_ptrs(h);
   p.state = state;
   p.v = v;
   p.f = forces;
-  for (int s = 0; s < n && h->it < h->cfg.nt; ++s) {
+  int done = 0;
+  for (; done < n && h->it < h->cfg.nt; ++done) {
     if (h->R > 0) {
       CK(h, launch_receivers(h->c, v, h->d_rec_elem, h->d_rec_ev, h->d_rec_w, h->d_seis, h->R, h->d_it, h->st));
       ++h->launches;
@@ -1447,6 +1462,7 @@ extern "C" int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int
     ++h->launches;
     h->it += 1;
   }
+  if (done > 0 && h->c.lean) h->ext_mirrors_stale = true;
   CK(h, cudaStreamSynchronize(h->st));
   return check_device_error(h);
 }
