@@ -76,57 +76,54 @@ def test_driver_builds_and_reports_missing_gpu(native, tmp_path):
     assert res.returncode == 1 and "no CUDA device" in res.stderr
 
 
-def test_fortran_interface_block_covers_header():
-    """INTEGRATION.md's ISO_C_BINDING module declares every entry point of the header,
-    with the header's return kind."""
+def _header():
     import re
     h = open(os.path.join(ROOT, "include", "ses3d_gpu.h")).read()
     decl = dict((name, ret) for ret, name in re.findall(r"^(const char \*|void \*|int64_t|long|int) ?(ses3d_gpu_\w+)\(",
                                                         h, re.M))
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    a = doc.index("```fortran")
-    block = doc[a:doc.index("```", a + 10)]
+    return h, decl
+
+
+def test_fortran_module_covers_header():
+    """include/ses3d_gpu.f90 (the ISO_C_BINDING module) declares every entry point of the
+    header with the header's return kind."""
+    import re
+    h, decl = _header()
+    mod = open(os.path.join(ROOT, "include", "ses3d_gpu.f90")).read()
     fort = dict((name, kind) for kind, name in re.findall(r"(integer\(c_\w+\)|type\(c_ptr\)) function (ses3d_gpu_\w+)",
-                                                          block))
+                                                          mod))
     assert set(decl) == set(fort), sorted(set(decl) ^ set(fort))
     want = {"int": "integer(c_int)", "long": "integer(c_long)", "int64_t": "integer(c_int64_t)",
             "const char *": "type(c_ptr)", "void *": "type(c_ptr)"}
     for name, ret in decl.items():
         assert fort[name] == want[ret], (name, ret, fort[name])
+    for name in decl:   # every interface binds the C name and ends
+        assert re.search(r"function %s\([^)]*\) bind\(c\)" % name, mod), name
 
 
-@pytest.mark.parametrize("field,value,fragment", [("nt", 0, b"nt"), ("dt", 0.0, b"dt"), ("adjoint_flag", 3, b"adjoint_flag"),
-                                                  ("is_diss", 2, b"is_diss"), ("n_events", 0, b"n_events")])
-def test_create_validates_before_touching_a_device(native, field, value, fragment):
-    """Configuration errors are reported before any device call (so also without a GPU)."""
-    from ses3d_gb300 import _lib
-    from ses3d_gb300 import synth
-    from ses3d_gb300.solver import config_from
-    p = synth.make_problem("tiny", nt=5, model=False)
-    cfg = config_from(p.box, p.setup, 5, p.events[0].event.dt, p.tau, p.D, pml=3)
-    setattr(cfg, field, value)
-    h = ctypes.c_void_p()
-    assert native.ses3d_gpu_create(ctypes.byref(cfg), ctypes.byref(h)) == -1
-    assert fragment in native.ses3d_gpu_last_error(None)
+def test_fortran_module_constants_match_header():
+    """Status codes, field and kernel identifiers of the Fortran module equal the header's."""
+    import re
+    h, _ = _header()
+    mod = open(os.path.join(ROOT, "include", "ses3d_gpu.f90")).read()
+    fort = {k: int(v) for k, v in re.findall(r"(SES3D_\w+) = (-?\d+)", mod)}
+    codes = {k: int(v) for k, v in re.findall(r"#define (SES3D_\w+) \(?(-?\d+)\)?", h)}
+    for k, v in codes.items():
+        assert fort[k] == v, k
+    for enum in re.findall(r"enum \{([^}]*)\}", h):
+        names = re.findall(r"(SES3D_(?:FIELD|KERNEL)_\w+)", re.sub(r"/\*.*?\*/", "", enum, flags=re.S))
+        for i, k in enumerate(n for n in names if not n.endswith("_COUNT")):
+            assert fort[k] == i, k
 
 
-def test_misfit_gradient_validates_arguments(native):
-    from ses3d_gb300 import _lib
-    from ses3d_gb300 import synth
-    from ses3d_gb300.solver import config_from
-    p = synth.make_problem("tiny", nt=5, model=False)
-    cfg = config_from(p.box, p.setup, 5, p.events[0].event.dt, p.tau, p.D, pml=3)
-    dummy = ctypes.c_void_p(16)  # never dereferenced: the checks fail first
-    assert native.ses3d_gpu_misfit_gradient_device(ctypes.byref(cfg), None, 1.0, None, dummy, 0) == -1
-    assert b"null" in native.ses3d_gpu_last_error(None)
-    cfg.lpd = 5
-    assert native.ses3d_gpu_misfit_gradient_device(ctypes.byref(cfg), dummy, 1.0, None, dummy, 0) == -1
-    assert b"lpd" in native.ses3d_gpu_last_error(None)
-
-
-def test_select_device_without_gpu_fails_cleanly(native):
-    import torch
-    if torch.cuda.is_available():
-        pytest.skip("a GPU is present")
-    assert native.ses3d_gpu_select_device(0) == -7
-    assert b"no CUDA device" in native.ses3d_gpu_last_error(None)
+def test_fortran_driver_calls_declared_entry_points():
+    """The Fortran driver calls only entry points the module declares, and its build
+    recipe names the module and the library."""
+    import re
+    mod = open(os.path.join(ROOT, "include", "ses3d_gpu.f90")).read()
+    drv = open(os.path.join(ROOT, "ses3d_gb300", "fortran", "ses3d_gpu_main.f90")).read()
+    declared = set(re.findall(r"function (ses3d_gpu_\w+)", mod))
+    used = set(re.findall(r"(ses3d_gpu_\w+)\(", drv))
+    assert used and used <= declared, sorted(used - declared)
+    mk = open(os.path.join(ROOT, "ses3d_gb300", "fortran", "Makefile")).read()
+    assert "ses3d_gpu.f90" in mk and "-lses3d_gpu" in mk
