@@ -14,7 +14,8 @@
       writes MODELS/MODELS (boxfile, per-rank records) and DATA/COORDINATES for the tree's
       INPUT/setup (generate_models.f90), optionally adding the block-model perturbations of
       MODELS/MODELS_3D (add_perturbation.f90). TABLE: one layer per line, top depth [km],
-      rho [g/cm^3], vp, vs [km/s][, Q]; without it the homogeneous model (model_type 1).
+      rho [g/cm^3], vp, vs [km/s][, Q]; without it the setup's model_type (1 homogeneous,
+      2 isotropic PREM, 3 homogeneous + QL6 Q, 4 EUMOD background, 7 ak135).
 """
 import argparse
 import json

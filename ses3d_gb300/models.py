@@ -11,11 +11,10 @@
 All arithmetic is FP32 in the reference's expression order, so the records equal what the
 Fortran programs write.
 
-The reference's built-in 1-D Earth models (PREM, ak135, EUMOD, QL6 attenuation;
-MODELS/MODELS_1D) are published data tables and are not transcribed here: the background is
-any callable `profile(z)` of the GLL radii giving (rho [g/cm^3], vp [km/s], vs [km/s],
-Q), converted exactly as those routines convert theirs (MODELS_1D/prem_iso.f90:214-228).
-`homogeneous` is the reference's model_type 1 (rho = 1, all moduli zero), and
+The background is the setup's model_type (`builtin_model`: homogeneous, isotropic PREM,
+homogeneous + QL6 Q, EUMOD, ak135 from ses3d_gb300.earth_models, MODELS/MODELS_1D) or any
+callable `profile(z)` of the GLL radii giving (rho [g/cm^3], vp [km/s], vs [km/s], Q),
+converted exactly as those routines convert theirs (MODELS_1D/prem_iso.f90:214-228);
 `LayeredProfile` builds a piecewise-constant profile from a depth table.
 """
 from __future__ import annotations
@@ -127,11 +126,20 @@ def profile_model(box: F.Box, profile: Profile, is_diss: int) -> Dict[str, np.nd
     (MODELS_1D/prem_iso.f90:214-228): units x1000, rhoinv = 1/rho, mu = cs cs rho,
     lambda = (cp cp - 2 cs cs) rho, A = B = C = 0."""
     x, y, z = box_axes(box)
-    ex, ey, ez = box.nx + 1, box.ny + 1, box.nz + 1
     rho, cp, cs, q = (np.asarray(v, np.float32) for v in profile(z))
     rho = (f32(1000.0) * rho).astype(np.float32)
     cp = (f32(1000.0) * cp).astype(np.float32)
     cs = (f32(1000.0) * cs).astype(np.float32)
+    return records_from_si(box, rho, cp, cs, q, is_diss)
+
+
+def records_from_si(box: F.Box, rho, cp, cs, q, is_diss: int) -> Dict[str, np.ndarray]:
+    """MODELS records from a 1-D model in SI units on the box's (nz+1, 5) radii:
+    rhoinv = 1/rho, mu = cs cs rho, lambda = (cp cp - 2 cs cs) rho, Q, A = B = C = 0, each
+    constant over (i, j, in, jn) (MODELS_1D/prem_iso.f90:214-228)."""
+    ex, ey, ez = box.nx + 1, box.ny + 1, box.nz + 1
+    x, y, z = box_axes(box)
+    rho, cp, cs = (np.asarray(v, np.float32).reshape(ez, 5) for v in (rho, cp, cs))
     rhoinv1 = (f32(1) / rho).astype(np.float32)
     mu1 = ((cs * cs).astype(np.float32) * rho).astype(np.float32)
     lam1 = (((cp * cp).astype(np.float32) - (f32(2) * cs * cs).astype(np.float32)).astype(np.float32)
@@ -148,16 +156,45 @@ def profile_model(box: F.Box, profile: Profile, is_diss: int) -> Dict[str, np.nd
     return out
 
 
+MODEL_TYPES = {1: "homogeneous", 2: "prem_iso", 3: "homogeneous_plus_Q", 4: "eumod_bg", 7: "ak135"}
+
+
+def builtin_model(box: F.Box, model_type: int, is_diss: int) -> Dict[str, np.ndarray]:
+    """The MODELS records of one box for the setup's model_type (generate_models.f90:389-417):
+    1 homogeneous, 2 isotropic PREM, 3 homogeneous + QL6 Q, 4 EUMOD background, 7 ak135
+    (ses3d_gb300.earth_models). Q is part of the records only with attenuation, as
+    generate_models writes it (generate_models.f90:436-453); type 1 leaves it at zero."""
+    from . import earth_models as EM
+    if model_type not in MODEL_TYPES:
+        raise ValueError("model_type %d is not one of the reference's 1-D models %s" % (model_type, sorted(MODEL_TYPES)))
+    if model_type == 1:
+        return homogeneous(box, is_diss)
+    _, _, z = box_axes(box)
+    if model_type == 3:
+        out = homogeneous(box, is_diss)
+        if is_diss:
+            ex, ey, ez = box.nx + 1, box.ny + 1, box.nz + 1
+            _, _, Z = _grid(np.zeros((ex, 5), np.float32), np.zeros((ey, 5), np.float32),
+                            EM.ql6(z, is_diss).reshape(ez, 5), ex, ey, ez)
+            out["Q"] = np.ascontiguousarray(Z, np.float32)
+        return out
+    fn = {2: EM.prem_iso, 4: EM.eumod_bg, 7: EM.ak135}[model_type]
+    rho, vp, vs, q = fn(z, is_diss)
+    return records_from_si(box, rho, vp, vs, q, is_diss)
+
+
 def generate_models(setup: F.Setup, root: str, profile: Optional[Profile] = None,
                     coordinates: bool = True) -> List[F.Box]:
     """generate_models: boxfile, coordinate files and per-rank model records of a SES3D tree
-    under root (MODELS/MODELS/, DATA/COORDINATES/). profile None: the homogeneous model."""
+    under root (MODELS/MODELS/, DATA/COORDINATES/). profile None: the setup's model_type
+    (builtin_model)."""
     boxes = F.make_boxes(setup)
     mdir = os.path.join(root, "MODELS", "MODELS")
     os.makedirs(mdir, exist_ok=True)
     F.write_boxfile(os.path.join(mdir, "boxfile"), boxes, setup.px, setup.py, setup.pz)
     for r, b in enumerate(boxes):
-        m = homogeneous(b, setup.is_diss) if profile is None else profile_model(b, profile, setup.is_diss)
+        m = (builtin_model(b, setup.model_type, setup.is_diss) if profile is None
+             else profile_model(b, profile, setup.is_diss))
         F.write_model(mdir, r, m)
         if coordinates:
             write_coordinates(os.path.join(root, "DATA", "COORDINATES"), r, b)
