@@ -162,6 +162,20 @@ def cpu_baseline(problem, steps):
                                       "step; set-up excluded" % (steps, problem.label, problem.n_nodes)}
 
 
+def workload_config(p):
+    """The workload description both arms print as `config` (identical for the same
+    --workload and --seed): sizes and inputs only, nothing measured."""
+    ex, ey, ez = p.nx + 1, p.ny + 1, p.nz + 1
+    N = p.n_nodes
+    G = (4 * ex + 1) * (4 * ey + 1) * (4 * ez + 1)
+    state_gb = 36 * 4 * N / 1e9
+    return {"workload": "%s: plain 3-D forward, %dx%dx%d elements, lpd 4, %d GLL points, anelastic (3 SLS), "
+                        "PML %d, 1 moment-tensor source, %d receivers" %
+                        (p.label, ex, ey, ez, N, p.pml, len(p.events[0].receivers.names)),
+            "gll_points": N, "unique_nodes": G,
+            "l2": "inputs larger than L2 (%.1f GB field state), no flush" % state_gb}
+
+
 def run_ours(args, rank, world, local):
     import numpy as np
     import torch
@@ -274,18 +288,15 @@ def run_ours(args, rank, world, local):
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "%s: plain 3-D forward, %dx%dx%d elements, lpd 4, %d GLL points, anelastic "
-                               "(3 SLS), PML 3, 1 moment-tensor source, %d receivers" %
-                               (args.workload, ex, ey, ez, N, len(p.events[0].receivers.names)),
-                   "gll_points": N, "unique_nodes": G, "elements_per_cta": args.epb,
-                   "graph_steps": args.graph, "l2": "inputs larger than L2 (6.6 GB state), no flush",
-                   "lean": bool(args.lean), "non_pml_element_fraction": (E - n_pml_el) / E,
-                   "step_algorithmic_bytes_per_point": step_bytes / N,
-                   "step_algorithmic_bytes_per_point_full_state": STATE_B + MAT_B + UNIQ_B * r_u,
-                   "step_achieved_gbs": step_gbs, "step_frac_of_peak": step_gbs / peak,
-                   "finite": finite, "steps_completed": steps_done,
-                   "kernel_ms": {"k_element": el_avg, "k_node": nd_ms / max(nd_n, 1),
-                                 "k_receivers": rc_ms / max(rc_n, 1)}},
+        "config": workload_config(p),
+        "run_details": {"elements_per_cta": args.epb, "graph_steps": args.graph,
+                        "lean": bool(args.lean), "non_pml_element_fraction": (E - n_pml_el) / E,
+                        "step_algorithmic_bytes_per_point": step_bytes / N,
+                        "step_algorithmic_bytes_per_point_full_state": STATE_B + MAT_B + UNIQ_B * r_u,
+                        "step_achieved_gbs": step_gbs, "step_frac_of_peak": step_gbs / peak,
+                        "finite": finite, "steps_completed": steps_done,
+                        "kernel_ms": {"k_element": el_avg, "k_node": nd_ms / max(nd_n, 1),
+                                      "k_receivers": rc_ms / max(rc_n, 1)}},
         "roofline": {"bound": "hbm", "kernel": "k_element", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes_per_launch": elem_bytes,
@@ -473,14 +484,16 @@ def run_gradient(args):
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the oracle (the reference solver restated on the CPU, FP32,
+    OpenMP on every host core) stepping the same workload as the GPU arm, --warmup untimed
+    steps and then --steps timed ones. Under torchrun only rank 0 runs it."""
     from ses3d_gb300 import synth
     if rank != 0:
         return None
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
-    steps = max(1, min(args.steps, args.cpu_steps))
-    warm = max(1, min(args.warmup, 1))
+    steps, warm = args.steps, args.warmup
     p = synth.make_problem(args.workload, nt=steps + warm + 1, seed=args.seed)
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
@@ -496,7 +509,7 @@ def run_reference(args, rank, world):
     return {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world, "steps": steps, "warmup": warm,
             "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": {"workload": args.workload, "gll_points": p.n_nodes},
+            "config": workload_config(p),
             "cpu_baseline": {"value": v, "unit": METRIC, "cores": int(os.environ["OMP_NUM_THREADS"]),
                              "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -505,7 +518,7 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2")

@@ -8,8 +8,11 @@ import pytest
 from ses3d_gb300 import formats as F
 from ses3d_gb300 import synth
 
-REF = "/root/reference"
-needs_ref = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "INPUT")), reason="reference tree not present")
+# the reference project's root (its example INPUT files are the parser fixtures); the tests
+# that read them are skipped when SES3D_REFERENCE_ROOT does not name a reference tree
+REF = os.environ.get("SES3D_REFERENCE_ROOT", "")
+needs_ref = pytest.mark.skipif(not (REF and os.path.isdir(os.path.join(REF, "INPUT"))),
+                               reason="SES3D_REFERENCE_ROOT does not name the reference tree")
 
 
 @needs_ref

@@ -10,7 +10,9 @@ from ses3d_gb300 import formats as F
 from ses3d_gb300 import models as M
 from ses3d_gb300 import synth
 
-REF_BLOCKS = "/root/reference/MODELS/MODELS_3D"
+# block-model fixtures of the reference project (MODELS/MODELS_3D), read when
+# SES3D_REFERENCE_ROOT names the reference tree
+REF_BLOCKS = os.path.join(os.environ.get("SES3D_REFERENCE_ROOT", "/nonexistent"), "MODELS", "MODELS_3D")
 
 
 def test_box_axes_match_solver_geometry():
