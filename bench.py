@@ -188,7 +188,7 @@ def run_ours(args, rank, world, local):
     barrier(world)
     from ses3d_gb300.solver import select_device
     select_device(local if world > 1 else 0)   # the library's runtime follows torch's device
-    nt = args.warmup + args.steps + 8  # the block-shape autotune spends 6 of the warm-up steps
+    nt = args.warmup + args.steps + 32  # the block-shape autotuner spends up to 27 warm-up steps
     p = synth.make_problem(args.workload, nt=nt, seed=args.seed)
     N = p.n_nodes
     ex, ey, ez = p.nx + 1, p.ny + 1, p.nz + 1
@@ -203,11 +203,14 @@ def run_ours(args, rank, world, local):
     DU_B = 96.0  # 9 displacement gradients + 3 mirror stresses, read + written
     sim = Simulation.from_problem(p)
     sim.set_lean(args.lean)
+    tuned = None
+    args.autotuned = not args.epb
     if args.epb:
         sim.set_block_elements(args.epb)
-    else:  # the library's block-shape autotuner, on a few warm-up steps
+    else:  # the library's block-shape autotuner, on warm-up steps
         tuned = sim.autotune(steps_each=2)
-        args.epb = min(tuned, key=tuned.get)
+        args.epb = tuned["chosen"]["elements_per_cta"]
+    shape = sim.shape
     if args.graph:
         sim.use_graph(True, args.graph)
     # warm-up (the autotune steps above count towards it)
@@ -240,6 +243,7 @@ def run_ours(args, rank, world, local):
     prof = Simulation.from_problem(p)
     prof.set_lean(args.lean)
     prof.set_block_elements(args.epb)
+    prof.set_kernel_shape(shape["element_shape"], shape["node_block"])
     prof.step(2)
     prof.profile(True)
     prof.step(args.prof_steps)
@@ -268,6 +272,8 @@ def run_ours(args, rank, world, local):
         t0 = time.perf_counter()
         cfg_sim = Simulation.from_problem(p, nt=args.steps, model=False)
         cfg_sim.set_lean(args.lean)
+        cfg_sim.set_block_elements(args.epb)
+        cfg_sim.set_kernel_shape(shape["element_shape"], shape["node_block"])
         cfg_sim.set_model(pinned)
         if args.graph:
             cfg_sim.use_graph(True, args.graph)
@@ -289,7 +295,8 @@ def run_ours(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(p),
-        "run_details": {"elements_per_cta": args.epb, "graph_steps": args.graph,
+        "run_details": {"elements_per_cta": args.epb, "kernel_shape": shape, "autotune": tuned,
+                        "graph_steps": args.graph,
                         "lean": bool(args.lean), "non_pml_element_fraction": (E - n_pml_el) / E,
                         "step_algorithmic_bytes_per_point": step_bytes / N,
                         "step_algorithmic_bytes_per_point_full_state": STATE_B + MAT_B + UNIQ_B * r_u,
@@ -311,6 +318,7 @@ def run_ours(args, rank, world, local):
         res["full_state"] = run_full_state(args, p, world, peak, STATE_B + MAT_B + UNIQ_B * r_u)
     if not args.no_batched:
         res["batched"] = run_batched(args, world)
+        res["forward_c1"] = run_forward_small(args, world)
     if rank == 0 and world == 1 and not args.no_grad:
         res["gradient"] = run_gradient(args)
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -323,10 +331,12 @@ def run_full_state(args, p, world, peak, bytes_per_point):
     stress read and written, as the reference does), timed the same way."""
     import torch
     from ses3d_gb300.solver import Simulation
-    warm = min(10, max(1, p.events[0].event.nt // 4))
-    steps = max(1, min(args.steps, 100, p.events[0].event.nt - warm))
     sim = Simulation.from_problem(p)
-    sim.set_block_elements(args.epb or 1)
+    tuned = sim.autotune(steps_each=2) if args.autotuned else None
+    if not args.autotuned:
+        sim.set_block_elements(args.epb)
+    warm = 3
+    steps = max(1, min(args.steps, 100, p.events[0].event.nt - sim.it - warm))
     if args.graph:
         sim.use_graph(True, args.graph)
     sim.step(warm)
@@ -342,7 +352,38 @@ def run_full_state(args, p, world, peak, bytes_per_point):
     gbs = p.n_nodes * bytes_per_point / (ms / 1e3) / 1e9
     return {"steps": steps, "ms_per_step": ms, "value": world * p.n_nodes / (ms / 1e3), "unit": METRIC,
             "step_algorithmic_bytes_per_point": bytes_per_point, "step_achieved_gbs": gbs,
-            "step_frac_of_peak": gbs / peak}
+            "step_frac_of_peak": gbs / peak, "kernel_shape": sim_shape(tuned)}
+
+
+def sim_shape(tuned):
+    return tuned["chosen"] if tuned else None
+
+
+def run_forward_small(args, world):
+    """The small plain-forward workload (22 x 22 x 10 elements, 605,000 GLL points), lean,
+    CUDA graph of 10 iterations, with its own autotuned block shapes."""
+    import torch
+    from ses3d_gb300 import synth
+    from ses3d_gb300.solver import Simulation
+    steps = 100
+    p = synth.make_problem("c1", nt=steps + 40, seed=args.seed)
+    sim = Simulation.from_problem(p)
+    sim.set_lean(True)
+    tuned = sim.autotune(steps_each=2)
+    sim.use_graph(True, 10)
+    sim.step(5)
+    stream = torch.cuda.ExternalStream(sim.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    sim.step(steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    sim.close()
+    return {"workload": "c1: 22x22x10 elements, %d GLL points, lean, CUDA graph of 10 iterations" % p.n_nodes,
+            "steps": steps, "ms_per_step": ms, "value": world * p.n_nodes / (ms / 1e3), "unit": METRIC,
+            "kernel_shape": tuned["chosen"], "autotune": tuned}
 
 
 def run_batched(args, world):
@@ -352,12 +393,12 @@ def run_batched(args, world):
     from ses3d_gb300 import synth
     from ses3d_gb300.solver import Simulation
     steps = args.batched_steps
-    out = {}
+    out, shapes = {}, {}
     for nev in (1, 16):
-        p = synth.make_problem("c4", nt=steps + 12, seed=args.seed, n_events=nev)
+        p = synth.make_problem("c4", nt=steps + 45, seed=args.seed, n_events=nev)
         sim = Simulation.from_problem(p)
         sim.set_lean(args.lean)
-        sim.set_block_elements(args.epb or 1)
+        shapes[nev] = sim.autotune(steps_each=2)["chosen"]
         sim.use_graph(True, 10)
         sim.step(10)
         stream = torch.cuda.ExternalStream(sim.stream)
@@ -375,19 +416,22 @@ def run_batched(args, world):
     return {"workload": "c4: 48x48x24 elements, %d GLL points per event, 16 events, receivers per event %d-%d, "
                         "CUDA graph of 10 iterations" % (n, min(nrec), max(nrec)),
             "events": 16, "ms_per_step": ms16, "value": world * 16 * n / (ms16 / 1e3), "unit": METRIC,
-            "single_event_ms_per_step": ms1, "per_event_speedup_vs_single": 16 * ms1 / ms16}
+            "single_event_ms_per_step": ms1, "per_event_speedup_vs_single": 16 * ms1 / ms16,
+            "kernel_shape_16_events": shapes[16], "kernel_shape_single_event": shapes[1]}
 
 
-def gradient_once(workload, nt, nev, seed, truth_kind):
+def gradient_once(workload, nt, nev, seed, truth_kind, memory_budget=None, exact=False):
     """One misfit gradient through the public autograd API (waveform_misfit forward +
     backward: forward run with records or checkpoints, misfit, adjoint sources, adjoint run,
-    kernel readout), timed end to end. Observed data come from a perturbed model (untimed)."""
+    kernel readout), timed end to end. Observed data come from a perturbed model (untimed).
+    memory_budget: device bytes the gradient may use (None: the free device memory).
+    exact: the exact discrete adjoint of the time stepping instead of the reference's kernels."""
     import numpy as np
     import torch
     from ses3d_gb300 import adjoint as A
     from ses3d_gb300 import synth
     p = synth.make_problem(workload, nt=nt, seed=seed, n_events=nev, adjoint_flag=1)
-    setup = A.MisfitSetup.from_problem(p, samp_ad=10)
+    setup = A.MisfitSetup.from_problem(p, samp_ad=10, memory_budget=memory_budget, exact=exact)
     m0 = A.problem_tensors(p)
     if truth_kind == "blob":    # +-5 % vs Gaussian blob, radius 150 km at 200 km depth
         truth = synth.build_model(p.box, blob=(0.05, 150e3, 200e3), is_diss=1)
@@ -403,13 +447,29 @@ def gradient_once(workload, nt, nev, seed, truth_kind):
     sec = time.perf_counter() - t0
     finite = bool(all(torch.isfinite(t.grad).all() for t in ms)) and bool(np.isfinite(float(chi.detach())))
     nrec = [len(e.receivers.names) for e in p.events]
+    plan = setup.last.get("plan")
     info = {"events": nev, "nt": nt, "samp_ad": 10, "gll_points_per_event": p.n_nodes,
+            "backward": "exact discrete adjoint" if exact else "reference kernels (ses3d_grad_Q)",
             "receivers_per_event": [min(nrec), max(nrec)],
+            "events_per_sub_batch": plan.events_per_batch if plan else nev,
             "records_per_checkpoint_segment": setup.last.get("records_per_segment", 0),
+            "records_per_checkpoint_subsegment": setup.last.get("records_per_subsegment", 0),
+            "memory_budget_bytes": memory_budget, "modeled_bytes_per_sub_batch": modeled_bytes(setup, plan),
+            "steps_per_checkpoint": setup.last.get("steps_per_checkpoint") if exact else None,
+            "steps_per_subsegment": setup.last.get("steps_per_subsegment") if exact else None,
             "seconds": sec, "s_per_event_gradient": sec / nev, "finite": finite}
     del setup, ms, chi
     torch.cuda.empty_cache()
     return info
+
+
+def modeled_bytes(setup, plan):
+    """Device bytes one sub-batch of the plan needs by the setup's memory model."""
+    if plan is None or setup.exact:
+        return None
+    m = setup.memory_model()
+    per = m["two_level"] if plan.K2 else (m["one_level"] if plan.K else m["keep"])
+    return m["shared"] + plan.events_per_batch * per
 
 
 def gradient_files_once(workload, nt, seed):
@@ -464,22 +524,30 @@ def gradient_files_once(workload, nt, seed):
 
 def run_gradient(args):
     """'s per event gradient': the 64x64x32 single-event gradient of the misfit workload at
-    its full length, and batched (16 events in one handle) against single-event gradients on
-    the 48x48x24 mesh and on the small 22x22x10 mesh over a shorter run."""
+    its full length; 16 events batched in one handle against single-event gradients on the
+    48x48x24 mesh (nt 3000) and the 22x22x10 mesh (nt 1000); two events of the 96x96x40
+    16-event gradient at nt 4000 under a 150 GB device-memory budget (two checkpoint
+    levels, one event per sub-batch); and the reference's file workflow on 48x48x24 against
+    the same gradient kept in HBM."""
     out = {"api": "ses3d_gb300.adjoint.waveform_misfit forward + backward (torch.autograd)",
            "dtype": "f32 fields, f64 kernel and misfit accumulation"}
     out["single_64x64x32"] = gradient_once("c3", args.grad_nt, 1, args.seed, "blob")
-    for wl, tag in (("c4", "48x48x24"), ("c1", "22x22x10")):
-        one = gradient_once(wl, args.grad_batched_nt, 1, args.seed, "checker")
-        many = gradient_once(wl, args.grad_batched_nt, 16, args.seed, "checker")
+    if not args.no_exact:
+        out["exact_64x64x32"] = gradient_once("c3", args.grad_nt, 1, args.seed, "blob", exact=True)
+    for wl, tag, nt in (("c4", "48x48x24", args.grad_c4_nt), ("c1", "22x22x10", args.grad_c1_nt)):
+        one = gradient_once(wl, nt, 1, args.seed, "checker")
+        many = gradient_once(wl, nt, 16, args.seed, "checker")
         out["single_" + tag] = one
         out["batched_" + tag] = many
         out["batched_per_event_speedup_vs_single_" + tag] = one["s_per_event_gradient"] / many["s_per_event_gradient"]
-        if wl == "c4":
-            files = gradient_files_once(wl, args.grad_batched_nt, args.seed)
-            out["single_files_" + tag] = files
-            out["batched_per_event_speedup_vs_single_files_" + tag] = (files["s_per_event_gradient"] /
-                                                                       many["s_per_event_gradient"])
+    if args.grad_c5_events > 0:
+        out["c5_96x96x40"] = gradient_once("c5", args.grad_c5_nt, args.grad_c5_events, args.seed, "checker",
+                                           memory_budget=150e9)
+    files = gradient_files_once("c4", args.grad_files_nt, args.seed)
+    hbm = gradient_once("c4", args.grad_files_nt, 1, args.seed, "checker")
+    out["single_files_48x48x24"] = files
+    out["single_hbm_48x48x24_same_nt"] = hbm
+    out["hbm_speedup_vs_files_48x48x24"] = files["s_per_event_gradient"] / hbm["s_per_event_gradient"]
     return out
 
 
@@ -534,7 +602,12 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=40)
     ap.add_argument("--no-grad", action="store_true")
     ap.add_argument("--grad-nt", type=int, default=4000, help="time steps of the 64x64x32 gradient")
-    ap.add_argument("--grad-batched-nt", type=int, default=200, help="time steps of the 48x48x24 gradients")
+    ap.add_argument("--no-exact", action="store_true", help="skip the exact-adjoint gradient")
+    ap.add_argument("--grad-c4-nt", type=int, default=3000, help="time steps of the 48x48x24 gradients")
+    ap.add_argument("--grad-c1-nt", type=int, default=1000, help="time steps of the 22x22x10 gradients")
+    ap.add_argument("--grad-c5-nt", type=int, default=4000, help="time steps of the 96x96x40 gradient")
+    ap.add_argument("--grad-c5-events", type=int, default=2, help="events of the 96x96x40 gradient timed (0: skip)")
+    ap.add_argument("--grad-files-nt", type=int, default=200, help="time steps of the file-workflow gradient")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

@@ -99,6 +99,12 @@ module ses3d_gpu_api
      integer(c_int) function ses3d_gpu_set_lean(h, enable) bind(c)
        import; type(c_ptr), value :: h; integer(c_int), value :: enable
      end function
+     integer(c_int) function ses3d_gpu_set_kernel_shape(h, element_shape, node_block) bind(c)
+       import; type(c_ptr), value :: h; integer(c_int), value :: element_shape, node_block
+     end function
+     integer(c_int) function ses3d_gpu_kernel_shape_count() bind(c)
+       import
+     end function
      integer(c_int) function ses3d_gpu_set_block_elements(h, elements_per_cta) bind(c)
        import; type(c_ptr), value :: h; integer(c_int), value :: elements_per_cta
      end function
@@ -153,6 +159,29 @@ module ses3d_gpu_api
      end function
      integer(c_int) function ses3d_gpu_set_checkpointing(h, records_per_segment) bind(c)
        import; type(c_ptr), value :: h; integer(c_int), value :: records_per_segment
+     end function
+     integer(c_int) function ses3d_gpu_set_checkpoint_levels(h, records_per_segment, records_per_subsegment) bind(c)
+       import; type(c_ptr), value :: h; integer(c_int), value :: records_per_segment, records_per_subsegment
+     end function
+     ! -- exact discrete adjoint
+     integer(c_int) function ses3d_gpu_exact_adjoint(h, steps_per_checkpoint, steps_per_subsegment) bind(c)
+       import; type(c_ptr), value :: h; integer(c_int), value :: steps_per_checkpoint, steps_per_subsegment
+     end function
+     integer(c_int) function ses3d_gpu_exact_set_seismogram_adjoint(h, ev, gx, gy, gz) bind(c)
+       import; type(c_ptr), value :: h; integer(c_int), value :: ev
+       real(c_float), intent(in) :: gx(*), gy(*), gz(*)
+     end function
+     integer(c_int) function ses3d_gpu_exact_backward(h) bind(c)
+       import; type(c_ptr), value :: h
+     end function
+     integer(c_int) function ses3d_gpu_exact_gradient(h, which, out, device) bind(c)
+       import; type(c_ptr), value :: h, out; integer(c_int), value :: which, device   ! out: host or device
+     end function
+     integer(c_int) function ses3d_gpu_exact_get_field(h, ev, field, out) bind(c)
+       import; type(c_ptr), value :: h; integer(c_int), value :: ev, field; real(c_float) :: out(*)
+     end function
+     integer(c_int) function ses3d_gpu_exact_set_field(h, ev, field, in) bind(c)
+       import; type(c_ptr), value :: h; integer(c_int), value :: ev, field; real(c_float), intent(in) :: in(*)
      end function
      integer(c_int) function ses3d_gpu_begin_adjoint(h) bind(c)
        import; type(c_ptr), value :: h

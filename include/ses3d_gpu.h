@@ -215,6 +215,16 @@ int ses3d_gpu_put_record(ses3d_gpu *h, int event, int record, const float *in);
  * run starts. Replaces the disk store/restore of SOURCE/ses3d_output.f90:5-267. */
 int ses3d_gpu_set_checkpointing(ses3d_gpu *h, int records_per_segment);
 
+/* Two checkpoint levels (records_per_subsegment = K2 with 0 < K2 < K): the flag-2 run
+ * recomputes a segment of K records once, keeping a full-state checkpoint before every
+ * K2-th of its records, and then each sub-segment of K2 records from those as the adjoint
+ * run reaches it (two extra forward passes in total). Memory per event: ceil(nrec / K)
+ * + ceil(K / K2) - 1 checkpoints, K2 records and one extra wavefield -- for 96 x 96 x 40,
+ * nt = 4000, samp_ad = 10 (401 records of 1.66 GB, checkpoints of 6.9 GB) K = 81, K2 = 9
+ * need 110 GB against 155 GB with one level. K2 = 0 is ses3d_gpu_set_checkpointing(h, K).
+ * Extends the disk store/restore of SOURCE/ses3d_output.f90:5-267 (no counterpart). */
+int ses3d_gpu_set_checkpoint_levels(ses3d_gpu *h, int records_per_segment, int records_per_subsegment);
+
 /* Device memory the handle holds now, in bytes. */
 int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h);
 
@@ -312,6 +322,38 @@ int ses3d_gpu_kernel_time(const ses3d_gpu *h, int which, double *total_ms, int64
  * routine is called. */
 int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int n);
 
+/* Exact discrete adjoint (no counterpart in the reference, whose ses3d_grad kernels are a
+ * continuous-adjoint approximation: SOURCE/ses3d_grad.f90:77-83). The backward run of a
+ * plain forward run is the transpose of its time step: the derivative of a misfit of the
+ * seismograms with respect to the model records is the gradient of the discrete forward
+ * run itself (what finite differences of the forward run converge to).
+ * Call ses3d_gpu_exact_adjoint on a flag-0 handle before stepping: the forward run keeps a
+ * full-state checkpoint every steps_per_checkpoint iterations (lean stepping must be off).
+ * After nt iterations, give each event's d misfit / d seismogram with
+ * ses3d_gpu_exact_set_seismogram_adjoint (gx, gy, gz: (nr, nt) each, receiver fastest, the
+ * layout of ses3d_gpu_get_seismograms; NULL = zero) and call ses3d_gpu_exact_backward: it
+ * recomputes one checkpoint segment at a time (one extra forward pass) and runs the adjoint
+ * iterations nt .. 1, accumulating the gradient in FP64. ses3d_gpu_exact_gradient returns
+ * the event-summed d misfit / d record for which = 0..6: rhoinv, mu, lambda, A, B, C, Q
+ * (N doubles, reference layout; device = 1: out is device memory on the handle's device).
+ * Memory per event: ceil(nt / K) checkpoints of (36 N + 3 G) floats, K iteration slots of
+ * (36 N + 6 G) floats, the adjoint state and 6 N + G doubles of gradient. With
+ * steps_per_subsegment = K2 (0 < K2 < K) a second level: each segment of K iterations is
+ * recomputed once into checkpoints every K2 iterations and each sub-segment of K2
+ * iterations from those (one more forward pass), so K2 slots and ceil(K / K2) - 1 more
+ * checkpoints instead of K slots (for 64 x 64 x 32, nt = 4000: K = 250, K2 = 16 need
+ * about 120 GB against 320 GB with one level).
+ * ses3d_gpu_exact_set_field / get_field access the adjoint state (field ids as
+ * ses3d_gpu_get_field, without MM_global): set before the backward run it is the adjoint of
+ * the final state (zero by default); read after it, the adjoint of the initial state. */
+int ses3d_gpu_exact_adjoint(ses3d_gpu *h, int steps_per_checkpoint, int steps_per_subsegment);
+int ses3d_gpu_exact_set_seismogram_adjoint(ses3d_gpu *h, int event, const float *gx, const float *gy,
+                                           const float *gz);
+int ses3d_gpu_exact_backward(ses3d_gpu *h);
+int ses3d_gpu_exact_gradient(ses3d_gpu *h, int which, double *out, int device);
+int ses3d_gpu_exact_get_field(ses3d_gpu *h, int event, int field, float *out);
+int ses3d_gpu_exact_set_field(ses3d_gpu *h, int event, int field, const float *in);
+
 /* Lean plain-forward stepping (adjoint_flag 0 only; off by default). Outside the PML
  * all profiles vanish, so (SOURCE/ses3d_evolution.f90:123-134,208-219) the displacement
  * gradients dxux..dzuy enter no output and the mirror stresses syx, szx, szy stay equal
@@ -326,8 +368,22 @@ int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int n);
 int ses3d_gpu_set_lean(ses3d_gpu *h, int enable);
 
 /* Element-kernel block shape: elements per CTA (1, 2 or 4); 0 selects the default.
- * bench.py's autotuner sets it. */
+ * 1 is the persistent bulk-copy kernel (plain and lean forward iterations), 2 and 4 the
+ * register-staged kernel. Simulation.autotune (ses3d_gb300/solver.py) searches it. */
 int ses3d_gpu_set_block_elements(ses3d_gpu *h, int elements_per_cta);
+
+/* Block shapes of the persistent element kernel and of the node kernel, selected at run
+ * time (each is a separately compiled instance; results are bit-identical across shapes):
+ * element_shape 0 .. ses3d_gpu_kernel_shape_count() - 1 =
+ *   0: 5 resident CTAs per SM (102 registers), next item's copy issued at the measured point
+ *   1: 4 CTAs per SM (128 registers)   2: 6 CTAs per SM (85 registers)
+ *   3: 5 CTAs per SM, copy issued at the other point (after the stress phase in lean
+ *      iterations, after the state read in full-state ones);
+ * node_block: threads per node-kernel CTA, 128, 256 (default) or 512. Defaults 0, 256.
+ * Simulation.autotune searches them per mesh and event count. No counterpart in the
+ * reference. */
+int ses3d_gpu_set_kernel_shape(ses3d_gpu *h, int element_shape, int node_block);
+int ses3d_gpu_kernel_shape_count(void);
 
 #ifdef __cplusplus
 }

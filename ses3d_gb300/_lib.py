@@ -80,6 +80,15 @@ SIGNATURES = {
     "ses3d_gpu_set_saving_vector": (c_int, [c_void_p, P_i]),
     "ses3d_gpu_begin_adjoint": (c_int, [c_void_p]),
     "ses3d_gpu_set_checkpointing": (c_int, [c_void_p, c_int]),
+    "ses3d_gpu_set_checkpoint_levels": (c_int, [c_void_p, c_int, c_int]),
+    "ses3d_gpu_set_kernel_shape": (c_int, [c_void_p, c_int, c_int]),
+    "ses3d_gpu_kernel_shape_count": (c_int, []),
+    "ses3d_gpu_exact_adjoint": (c_int, [c_void_p, c_int, c_int]),
+    "ses3d_gpu_exact_set_seismogram_adjoint": (c_int, [c_void_p, c_int, P_f, P_f, P_f]),
+    "ses3d_gpu_exact_backward": (c_int, [c_void_p]),
+    "ses3d_gpu_exact_gradient": (c_int, [c_void_p, c_int, c_void_p, c_int]),
+    "ses3d_gpu_exact_get_field": (c_int, [c_void_p, c_int, c_int, P_f]),
+    "ses3d_gpu_exact_set_field": (c_int, [c_void_p, c_int, c_int, P_f]),
     "ses3d_gpu_memory_bytes": (ctypes.c_int64, [c_void_p]),
     "ses3d_gpu_get_setup_int": (c_long, [c_void_p, c_int, c_char_p, P_i]),
     "ses3d_gpu_get_setup_real": (c_long, [c_void_p, c_int, c_char_p, P_f]),

@@ -18,6 +18,15 @@ quadrature volume; for Q_mu it is divided by Q. This is the continuous-adjoint g
 the reference (not the exact discrete adjoint of the time stepping); the test suite
 reports its agreement with central finite differences.
 
+Exact gradient (MisfitSetup.exact = True): the backward pass is the exact discrete adjoint
+of the forward time stepping (ses3d_gpu_exact_*): the forward run keeps full-state
+checkpoints every K iterations, the seismogram derivative dchi/du(t) = dt F^T F (u - d)(t)
+enters at the receivers, the library runs the transposed iterations nt .. 1 and returns
+dchi/d(rhoinv, mu, lambda, A, B, C, Q), and the chain rule through the record mapping
+(model_gradients_from_records) gives dchi/d(rho, vp, vsh, vsv, Q). It is the derivative of
+the computed misfit itself, which central finite differences of the forward run converge
+to.
+
 Adjoint source of a velocity misfit: a(t) = dchi/du_vel(t) = dt F^T F (u - d)(t); the
 force applied in adjoint iteration it is the time derivative of the time-reversed a
 (TOOLS/adjoint_source.py writes the reversed -d/dt of the velocity residual).
@@ -84,10 +93,11 @@ class EventData:
 @dataclass
 class MemoryPlan:
     """Sub-batches of `events_per_batch` events, checkpoint segment length K (0: keep
-    every record)."""
+    every record) and sub-segment length K2 (0: one checkpoint level)."""
     events_per_batch: int
     K: int
     n_events: int
+    K2: int = 0
 
     @property
     def groups(self) -> List[List[int]]:
@@ -105,6 +115,8 @@ class MisfitSetup:
     samp_ad: int = 10
     memory_budget: Optional[float] = None  # device bytes a gradient may use; None: free device memory
     grad_q: bool = True
+    exact: bool = False          # backward = exact discrete adjoint of the time stepping
+    checkpoint_steps: Optional[int] = None  # exact: forward iterations per checkpoint (None: planned)
     last: dict = field(default_factory=dict)
 
     @classmethod
@@ -130,9 +142,10 @@ class MisfitSetup:
         return c
 
     def simulate(self, records: dict, adjoint: bool = False, events: Optional[Sequence[int]] = None,
-                 K: Optional[int] = None) -> Simulation:
+                 K: Optional[int] = None, K2: int = 0) -> Simulation:
         """Forward run of the given events (default: all) on the model records (device
-        tensors). adjoint: keep the forward records, or checkpoints every K records."""
+        tensors). adjoint: keep the forward records, or checkpoints every K records (and,
+        with K2, second-level checkpoints every K2 records of a segment)."""
         evs = list(range(len(self.events))) if events is None else list(events)
         self.check_records(records)
         select_device(next(iter(records.values())).device.index or 0)  # the handle lives with the model
@@ -148,12 +161,67 @@ class MisfitSetup:
             sim.set_lean(True)        # seismograms only: the displacement gradients enter nothing
         if adjoint:
             if K is None:
-                K = self.plan().K
+                pl = self.plan()
+                K, K2 = pl.K, pl.K2
             if K:
-                L.check(sim.lib.ses3d_gpu_set_checkpointing(sim.h, K), sim.h)
+                L.check(sim.lib.ses3d_gpu_set_checkpoint_levels(sim.h, K, K2), sim.h)
             self.last["records_per_segment"] = K
+            self.last["records_per_subsegment"] = K2
         sim.run()
         return sim
+
+    def simulate_exact(self, records: dict, events: Sequence[int], K: int, K2: int = 0) -> Simulation:
+        """Plain forward run of the given events that keeps full-state checkpoints every K
+        iterations for the exact discrete adjoint (ses3d_gpu_exact_adjoint; with K2 a second
+        checkpoint level every K2 iterations of a segment)."""
+        self.check_records(records)
+        select_device(next(iter(records.values())).device.index or 0)
+        sim = Simulation(self._config(0, len(events)))
+        sim.set_model_device([records[k].data_ptr() if k in records else 0 for k in
+                              ("rhoinv", "mu", "lambda", "A", "B", "C", "Q")])
+        for slot, k in enumerate(events):
+            e = self.events[k]
+            sim.set_source(slot, e.xxs, e.yys, e.zzs, e.source_type, e.mom, e.stf)
+            sim.set_receivers(slot, e.recloc)
+        sim.exact_adjoint(K, K2)
+        sim.use_graph(True, 10)
+        sim.run()
+        return sim
+
+    def exact_plan(self) -> MemoryPlan:
+        """Events per sub-batch and checkpointing of the exact adjoint. Per event: the state,
+        velocity and forces, the adjoint state and its FP64 gradients, and either
+        ceil(nt / K) checkpoints and K iteration slots (one level, K ~ sqrt(nt)), or
+        ceil(nt / K) + ceil(K / K2) - 1 checkpoints and K2 slots (two levels, one more
+        recompute pass). The largest sub-batch that fits wins, with one level before two."""
+        c = self.cfg_template
+        E = (c.nx + 1) * (c.ny + 1) * (c.nz + 1)
+        N, G = 125.0 * E, float((4 * c.nx + 5) * (4 * c.ny + 5) * (4 * c.nz + 5))
+        nt = int(c.nt)
+        ckpt, slot = (36.0 * N + 3.0 * G) * 4, (36.0 * N + 6.0 * G) * 4
+        shared = 64.0 * N + 12.0 * G
+        event = (36.0 * N + 3.0 * G + 3.0 * N) * 4 + (39.0 * N + 6.0 * G) * 4 + (6.0 * N + G) * 8 + ckpt
+        if self.checkpoint_steps:
+            K = min(nt, self.checkpoint_steps)
+        else:
+            K = max(1, min(nt, int(round(math.sqrt(nt * ckpt / slot)))))
+        one = event + math.ceil(nt / K) * ckpt + K * slot
+        best = None
+        for K1 in range(2, nt + 1):
+            k2c = max(1, min(K1 - 1, int(round(math.sqrt(K1 * ckpt / slot)))))
+            for K2 in range(max(1, k2c - 1), min(K1 - 1, k2c + 1) + 1):
+                mem = math.ceil(nt / K1) * ckpt + (math.ceil(K1 / K2) - 1) * ckpt + K2 * slot
+                if best is None or mem < best[0]:
+                    best = (mem, K1, K2)
+        two = event + best[0] if best else one
+        budget = self.budget()
+        nev = len(self.events)
+        for g in range(nev, 0, -1):
+            if shared + g * one <= budget:
+                return MemoryPlan(g, K, nev)
+            if best and shared + g * two <= budget:
+                return MemoryPlan(g, best[1], nev, best[2])
+        return MemoryPlan(1, best[1], nev, best[2]) if best else MemoryPlan(1, K, nev)
 
     @property
     def n_points(self) -> int:
@@ -183,26 +251,30 @@ class MisfitSetup:
         return max(0.0, float(free) - max(8e9, 0.05 * float(total)))
 
     def plan(self) -> "MemoryPlan":
-        """Events per sub-batch and checkpoint segment length K (0: every record kept) so
-        that one sub-batch's device memory fits the budget. Per event: element state,
-        velocity and forces, FP64 kernel accumulators, and either every record (9 floats
-        per GLL point and stored iteration) or ceil(nrec / K) full-state checkpoints, K
-        records and a second wavefield; shared per handle: material, geometry, mass
-        matrix. The largest sub-batch that fits wins; K minimises checkpoint + segment
-        memory. With nothing fitting, one event per sub-batch with checkpoints."""
-        shared, keep, with_ckpt, K = self.memory_model()
+        """Events per sub-batch and checkpointing so that one sub-batch's device memory fits
+        the budget. Per event: element state, velocity and forces, FP64 kernel accumulators,
+        and either every record (9 floats per GLL point and stored iteration), or
+        ceil(nrec / K) full-state checkpoints, K records and a second wavefield (one level),
+        or ceil(nrec / K) + ceil(K / K2) - 1 checkpoints, K2 records and a second wavefield
+        (two levels); shared per handle: material, geometry, mass matrix. The storage with
+        the fewest recompute passes that fits wins (records kept, then one level, then two),
+        with the largest sub-batch it allows; K and K2 minimise memory. With nothing
+        fitting, one event per sub-batch with two levels."""
+        m = self.memory_model()
         budget = self.budget()
         nev = len(self.events)
-        for g in range(nev, 0, -1):
-            if shared + g * keep <= budget:
-                return MemoryPlan(g, 0, nev)
-            if shared + g * with_ckpt <= budget:
-                return MemoryPlan(g, K, nev)
-        return MemoryPlan(1, K, nev)
+        # a recompute pass costs a whole forward sweep, while batching saves a few per cent
+        # (the material traffic shared by the events): the fewest passes come first
+        for per, K, K2 in ((m["keep"], 0, 0), (m["one_level"], m["K"], 0), (m["two_level"], m["K1"], m["K2"])):
+            g = min(nev, int((budget - m["shared"]) // per)) if budget > m["shared"] else 0
+            if g >= 1:
+                return MemoryPlan(g, K, nev, K2)
+        return MemoryPlan(1, m["K1"], nev, m["K2"])
 
-    def memory_model(self):
-        """(bytes per handle, per event keeping every record, per event with checkpoints
-        every K records, K)."""
+    def memory_model(self) -> dict:
+        """Device bytes: per handle ("shared"), per event keeping every record ("keep"), with
+        one checkpoint level every K records ("one_level") and with two levels every K1 and
+        K2 records ("two_level"), and the K, K1, K2 that minimise those."""
         c = self.cfg_template
         E = (c.nx + 1) * (c.ny + 1) * (c.nz + 1)
         N, G = 125.0 * E, float((4 * c.nx + 5) * (4 * c.ny + 5) * (4 * c.nz + 5))
@@ -213,7 +285,16 @@ class MisfitSetup:
         rec = 36.0 * N
         ckpt = (36.0 * N + 3.0 * G) * 4
         K = max(1, int(round(math.sqrt(nrec * ckpt / rec))))
-        return shared, event + nrec * rec, event + ckpt + math.ceil(nrec / K) * ckpt + K * rec, K
+        one = event + ckpt + math.ceil(nrec / K) * ckpt + K * rec
+        best = None
+        for K1 in range(2, max(3, nrec + 1)):
+            k2c = max(1, min(K1 - 1, int(round(math.sqrt(K1 * ckpt / rec)))))
+            for K2 in range(max(1, k2c - 2), min(K1 - 1, k2c + 2) + 1):
+                mem = ckpt + math.ceil(nrec / K1) * ckpt + (math.ceil(K1 / K2) - 1) * ckpt + K2 * rec
+                if best is None or mem < best[0]:
+                    best = (mem, K1, K2)
+        return {"shared": shared, "keep": event + nrec * rec, "one_level": one, "K": K,
+                "two_level": event + best[0], "K1": best[1], "K2": best[2]}
 
     def filt(self, nt: int, dt: float) -> Bandpass:
         return Bandpass(nt, dt, self.fmin, self.fmax)
@@ -327,6 +408,42 @@ def misfit_gradients_device(cfg: L.Config, ksum: list, grad_out: float, Q) -> li
 
 
 KERNEL_NAMES = ("rho", "cp", "csh", "csv", "Q_mu")
+RECORD_NAMES = ("rhoinv", "mu", "lambda", "A", "B", "C", "Q")
+
+
+def record_gradients_device(sim: Simulation, device, acc: Optional[list] = None) -> list:
+    """d misfit / d model record (RECORD_NAMES; Q only with attenuation, else None) after an
+    exact backward run, FP64 tensors on `device`, added to `acc` (earlier sub-batches)."""
+    import torch
+    out = []
+    for i, nm in enumerate(RECORD_NAMES):
+        if nm == "Q" and not sim.cfg.is_diss:
+            out.append(None)
+            continue
+        t = torch.empty(sim.N, dtype=torch.float64, device=device)
+        sim.exact_gradient_device(nm, t.data_ptr())
+        out.append(t if acc is None else acc[i] + t)
+    return out
+
+
+def model_gradients_from_records(grec: list, rho, vp, vsh, vsv, Q, grad_out: float) -> list:
+    """Chain rule through model_records (mu = rho vsh^2, lambda = rho vp^2 - 2 mu,
+    B = rho vsv^2 - mu, rhoinv = 1 / rho; A = C = 0) in FP64: d misfit / d (rho, vp, vsh,
+    vsv, Q) from the gradients with respect to the records."""
+    import torch
+    with torch.enable_grad():
+        xs = [t.detach().double().requires_grad_(True) for t in (rho, vp, vsh, vsv, Q)]
+        r, p_, sh, sv, q = xs
+        mu = r * sh * sh
+        outs = [1.0 / r, mu, r * p_ * p_ - 2.0 * mu, r * sv * sv - mu, q]
+        gl = [grec[0], grec[1], grec[2], grec[4], grec[6]]
+        pairs = [(o, g) for o, g in zip(outs, gl) if g is not None]
+        gr = torch.autograd.grad([o for o, _ in pairs], xs, grad_outputs=[g for _, g in pairs], allow_unused=True)
+    out = []
+    for g, x in zip(gr, (rho, vp, vsh, vsv, Q)):
+        g = torch.zeros_like(x, dtype=torch.float64) if g is None else g
+        out.append((g * float(grad_out)).to(x.dtype))
+    return out
 
 
 class _Misfit:
@@ -340,13 +457,15 @@ class _Misfit:
             @staticmethod
             def forward(ctx, setup: MisfitSetup, rho, vp, vsh, vsv, Q):
                 recs = model_records(rho, vp, vsh, vsv, Q)
+                if setup.exact:
+                    return WaveformMisfit.forward_exact(ctx, setup, recs, rho, vp, vsh, vsv, Q)
                 plan = setup.plan()
                 setup.last["plan"] = plan
                 dt = float(setup.cfg_template.dt)
                 ctx.setup, ctx.dt, ctx.plan = setup, dt, plan
                 ctx.save_for_backward(Q)
                 if len(plan.groups) == 1:  # one handle keeps the forward records for backward
-                    sim = setup.simulate(recs, adjoint=True, K=plan.K)
+                    sim = setup.simulate(recs, adjoint=True, K=plan.K, K2=plan.K2)
                     syn = setup.seismograms(sim)
                     ctx.sim, ctx.syn, ctx.kernels = sim, syn, None
                 else:
@@ -355,7 +474,7 @@ class _Misfit:
                     # backward scales the summed kernels
                     syn, ksum = [], None
                     for grp in plan.groups:
-                        sim = setup.simulate(recs, adjoint=True, events=grp, K=plan.K)
+                        sim = setup.simulate(recs, adjoint=True, events=grp, K=plan.K, K2=plan.K2)
                         sg = setup.seismograms(sim)
                         srcs = setup.adjoint_sources(sg, dt, setup.last.get("shift", 0.0), events=grp)
                         for slot, k in enumerate(grp):
@@ -371,7 +490,59 @@ class _Misfit:
                 return torch.tensor(chi, dtype=torch.float64, device=rho.device)
 
             @staticmethod
+            def forward_exact(ctx, setup, recs, rho, vp, vsh, vsv, Q):
+                """Forward runs with exact-adjoint checkpoints; with one sub-batch the handle is
+                kept for backward, with several each sub-batch runs its backward here (an
+                event's seismogram adjoint depends on its own residual only)."""
+                plan = setup.exact_plan()
+                setup.last["plan"] = plan
+                setup.last["steps_per_checkpoint"] = plan.K
+                setup.last["steps_per_subsegment"] = plan.K2
+                dt = float(setup.cfg_template.dt)
+                ctx.setup, ctx.dt, ctx.plan = setup, dt, plan
+                ctx.save_for_backward(rho, vp, vsh, vsv, Q)
+                ctx.exact = True
+                syn, grec = [], None
+                ctx.sim = None
+                for grp in plan.groups:
+                    sim = setup.simulate_exact(recs, grp, plan.K, plan.K2)
+                    sg = setup.seismograms(sim)
+                    syn += sg
+                    if len(plan.groups) == 1:
+                        ctx.sim = sim
+                    else:
+                        WaveformMisfit.exact_backward(setup, sim, sg, grp, dt)
+                        grec = record_gradients_device(sim, rho.device, grec)
+                        sim.close()
+                ctx.syn, ctx.grec = syn, grec
+                chi = setup.misfit_value(syn, dt)
+                setup.last["seismograms"] = syn
+                return torch.tensor(chi, dtype=torch.float64, device=rho.device)
+
+            @staticmethod
+            def exact_backward(setup, sim, syn, events, dt):
+                """d chi / d seismogram = dt F^T F (u - d) per sample into the handle, then the
+                backward run."""
+                F = setup.filt(syn[0].shape[-1], dt)
+                for slot, (k, s) in enumerate(zip(events, syn)):
+                    g = dt * F(F(s - setup.events[k].observed))        # (3, nr, nt)
+                    sim.set_seismogram_adjoint(slot, g[0], g[1], g[2])
+                sim.exact_backward()
+
+            @staticmethod
             def backward(ctx, grad_out):
+                if getattr(ctx, "exact", False):
+                    rho, vp, vsh, vsv, Q = ctx.saved_tensors
+                    grec = ctx.grec
+                    if ctx.sim is not None:
+                        WaveformMisfit.exact_backward(ctx.setup, ctx.sim, ctx.syn, ctx.plan.groups[0], ctx.dt)
+                        grec = record_gradients_device(ctx.sim, Q.device)
+                        ctx.sim.close()
+                        ctx.sim = None
+                    ctx.setup.last["record_gradients"] = dict(zip(RECORD_NAMES, grec))
+                    grads = model_gradients_from_records(grec, rho, vp, vsh, vsv, Q, float(grad_out))
+                    ctx.setup.last["kernels"] = {n: g for n, g in zip(("rho", "vp", "vsh", "vsv", "Q"), grads)}
+                    return (None,) + tuple(grads)
                 (Q,) = ctx.saved_tensors
                 setup, syn, dt = ctx.setup, ctx.syn, ctx.dt
                 if ctx.kernels is None:

@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall",
              "-I" + os.path.join(ROOT, "include")]
 
-CU_SOURCES = ["kernels.cu", "capi.cu"]
+CU_SOURCES = ["kernels.cu", "adjoint.cu", "capi.cu"]
 CXX_SOURCES = ["setup.cpp"]
 DRIVER_SOURCES = ["driver.cpp", "formats.cpp"]
 

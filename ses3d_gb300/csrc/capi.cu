@@ -24,8 +24,9 @@ struct Range {
 }  // namespace
 
 namespace ses3d {
-cudaError_t launch_element(int diss, int mode, int epb, const Consts &c, const Ptrs &p, cudaStream_t st);
-cudaError_t launch_node(const Consts &c, const Ptrs &p, cudaStream_t st);
+cudaError_t launch_element(int diss, int mode, int epb, int shape, const Consts &c, const Ptrs &p, cudaStream_t st);
+cudaError_t launch_node(int node_block, const Consts &c, const Ptrs &p, cudaStream_t st);
+int element_shape_count();
 cudaError_t launch_receivers(const Consts &c, const float *v, const int *rec_elem, const int *rec_ev,
                              const float *rec_w, float *seis, int R, const int *d_it, cudaStream_t st);
 cudaError_t launch_inject(const Consts &c, float *f, const int4 *groups, int ngroups, const float *delta,
@@ -48,6 +49,12 @@ cudaError_t launch_wait_selftest(int *err, unsigned long long limit_ns, cudaStre
 cudaError_t launch_sum_events_d(const double *grad, int slot, int nev, long long N, double *out, cudaStream_t st);
 cudaError_t launch_pack_mat(const float *ref, float *out, long long E, cudaStream_t st);
 cudaError_t launch_state_field(float *state_ev, int field, float *ref, long long E, int to_ref, cudaStream_t st);
+cudaError_t launch_adjoint_node1(const Consts &c, const Ptrs &p, const AdjPtrs &a, cudaStream_t st);
+cudaError_t launch_adjoint_node2(const Consts &c, const AdjPtrs &a, cudaStream_t st);
+cudaError_t launch_adjoint_element(int diss, const Consts &c, const Ptrs &p, const AdjPtrs &a, cudaStream_t st);
+cudaError_t launch_adjoint_model_gradient(const Consts &c, const Ptrs &p, const double *gmat, const double *gimm,
+                                          int which, int is_diss, double sD, const float *z, const float *sinx,
+                                          const float *w, double *out, cudaStream_t st);
 }  // namespace ses3d
 
 using namespace ses3d;
@@ -91,6 +98,8 @@ struct ses3d_gpu {
   int mode_flag = 0;  // current adjoint_flag
   bool model_set = false;
   int epb = 1;
+  int shape = 0;        // block shape of the persistent element kernel
+  int node_block = 256;  // threads per CTA of the node kernel
   long long launches = 0;
   Consts c;
   // device memory
@@ -128,8 +137,29 @@ struct ses3d_gpu {
   int ckpt_K = 0;
   std::vector<float *> ckpts;     // each [nev][NSTATE N + 3 G]
   std::vector<int> ckpt_it;       // completed iterations at each checkpoint
-  std::vector<float *> segbuf;    // ckpt_K records of the recomputed segment
+  std::vector<float *> segbuf;    // the records of the recomputed (sub-)segment
   int seg_loaded = -1;
+  // second level (ckpt_K2 > 0): a segment of ckpt_K records is recomputed once into
+  // checkpoints before every ckpt_K2-th of its records, and each sub-segment of ckpt_K2
+  // records is recomputed from those when the adjoint run reaches it
+  int ckpt_K2 = 0;
+  std::vector<float *> ckpt2;     // checkpoints of sub-segments 1.. of the loaded segment
+  std::vector<int> ckpt2_it;
+  int sub_loaded = -1;            // sub-segment of seg_loaded whose records are in segbuf
+  // exact discrete adjoint (ses3d_gpu_exact_*): full-state checkpoints of the plain forward
+  // run every ex_K iterations; the backward run recomputes one segment at a time into
+  // per-iteration slots (state, velocity, assembled forces) and steps the adjoint through it
+  int ex_K = 0;
+  int ex_K2 = 0;                           // two levels: a segment is recomputed into checkpoints every ex_K2
+  std::vector<float *> ex_ckpts;           // at completed iterations 0, ex_K, 2 ex_K, ...
+  std::vector<float *> ex_ckpts2;          // second-level checkpoints of the segment being reversed
+  std::vector<float *> ex_slots;
+  float *d_astate = nullptr, *d_av = nullptr, *d_aF = nullptr, *d_af = nullptr;
+  double *d_egmat = nullptr, *d_egimm = nullptr;
+  int *d_ait = nullptr;
+  std::vector<std::vector<float>> seis_adj;  // per event: d misfit / d seismogram, [3][nt][nr]
+  ForceSet fseis;                            // the receivers' adjoint sources as point forces
+  bool ex_done = false;
   float *d_state2 = nullptr, *d_v2 = nullptr;  // wavefield of the recomputing forward run
   int *d_it2 = nullptr;
   std::vector<int> saving_vector;  // [nt+1]
@@ -395,8 +425,9 @@ Wave primary_wave(ses3d_gpu *h) {
 }
 
 // one iteration of a wavefield: receivers, element, inject, node (+ record / kernel work)
-int launch_iteration(ses3d_gpu *h, const Wave &w, int mode, float *rec, bool timed = false) {
+int launch_iteration(ses3d_gpu *h, const Wave &w, int mode, float *rec, bool timed = false, float *fg = nullptr) {
   Ptrs p = make_ptrs(h);
+  p.fg = fg;
   p.state = w.state;
   p.v = w.v;
   p.d_it = w.d_it;
@@ -410,7 +441,7 @@ int launch_iteration(ses3d_gpu *h, const Wave &w, int mode, float *rec, bool tim
   }
   {
     Timed t(h, 0, timed);
-    CK(h, launch_element(h->cfg.is_diss, mode, h->epb, h->c, p, h->st));
+    CK(h, launch_element(h->cfg.is_diss, mode, h->epb, h->shape, h->c, p, h->st));
     ++h->launches;
   }
   if (F.n) {
@@ -420,7 +451,7 @@ int launch_iteration(ses3d_gpu *h, const Wave &w, int mode, float *rec, bool tim
   }
   {
     Timed t(h, 1, timed);
-    CK(h, launch_node(h->c, p, h->st));
+    CK(h, launch_node(h->node_block, h->c, p, h->st));
     ++h->launches;
   }
   return SES3D_OK;
@@ -444,43 +475,148 @@ int save_checkpoint(ses3d_gpu *h, int completed_it) {
   return SES3D_OK;
 }
 
-// Recomputes the records of segment s (records s K .. min((s+1) K, nrec) - 1) into segbuf
-// by a forward run from checkpoint s on the second wavefield.
-int recompute_segment(ses3d_gpu *h, int s) {
-  Range range_("ses3d recompute segment");
+// Full-state checkpoint of the primary wavefield for the exact adjoint (completed
+// iterations = 0, ex_K, 2 ex_K, ...); kept for the whole run.
+int save_exact_checkpoint(ses3d_gpu *h, int completed_it) {
+  const int idx = completed_it / h->ex_K;
   const size_t ns = (size_t)h->cfg.n_events * NSTATE * h->geo.N;
   const size_t nv = (size_t)h->cfg.n_events * 3 * h->geo.G;
-  const size_t rec_floats = (size_t)h->cfg.n_events * NREC * h->geo.N;
-  if (!h->d_state2) {
-    CK(h, dalloc(&h->d_state2, ns));
-    CK(h, dalloc(&h->d_v2, nv));
-    CK(h, dalloc(&h->d_it2, 1));
+  while ((int)h->ex_ckpts.size() <= idx) {
+    float *c = nullptr;
+    CK(h, dalloc(&c, ckpt_floats(h)));
+    h->ex_ckpts.push_back(c);
   }
-  while ((int)h->segbuf.size() < h->ckpt_K) {
+  CK(h, cudaMemcpyAsync(h->ex_ckpts[idx], h->d_state, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  CK(h, cudaMemcpyAsync(h->ex_ckpts[idx] + ns, h->d_v, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  return SES3D_OK;
+}
+
+// The second wavefield (the recomputing forward run), allocated on first use.
+int ensure_wave2(ses3d_gpu *h) {
+  if (h->d_state2) return SES3D_OK;
+  CK(h, dalloc(&h->d_state2, (size_t)h->cfg.n_events * NSTATE * h->geo.N));
+  CK(h, dalloc(&h->d_v2, (size_t)h->cfg.n_events * 3 * h->geo.G));
+  CK(h, dalloc(&h->d_it2, 1));
+  return SES3D_OK;
+}
+
+// Loads a full-state checkpoint (completed iterations it0) into the second wavefield.
+int load_wave2(ses3d_gpu *h, const float *ckpt, const int &it0) {
+  const size_t ns = (size_t)h->cfg.n_events * NSTATE * h->geo.N;
+  const size_t nv = (size_t)h->cfg.n_events * 3 * h->geo.G;
+  int rc = ensure_wave2(h);
+  if (rc) return rc;
+  CK(h, cudaMemcpyAsync(h->d_state2, ckpt, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  CK(h, cudaMemcpyAsync(h->d_v2, ckpt + ns, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  CK(h, cudaMemcpyAsync(h->d_it2, &it0, sizeof(int), cudaMemcpyHostToDevice, h->st));
+  return SES3D_OK;
+}
+
+// Runs the second wavefield from completed iteration it0 and stores records rA .. rB - 1
+// into segbuf[0 ..] (record iterations in MODE 1, the others plain).
+int recompute_records(ses3d_gpu *h, int it0, int rA, int rB) {
+  const size_t rec_floats = (size_t)h->cfg.n_events * NREC * h->geo.N;
+  if (!h->d_state2) return fail(h, SES3D_E_STATE, "the recomputing wavefield is not loaded");
+  while ((int)h->segbuf.size() < rB - rA) {
     float *r = nullptr;
     CK(h, dalloc(&r, rec_floats));
     h->segbuf.push_back(r);
   }
-  CK(h, cudaMemcpyAsync(h->d_state2, h->ckpts[s], ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
-  CK(h, cudaMemcpyAsync(h->d_v2, h->ckpts[s] + ns, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
-  int it0 = h->ckpt_it[s];
-  CK(h, cudaMemcpyAsync(h->d_it2, &h->ckpt_it[s], sizeof(int), cudaMemcpyHostToDevice, h->st));
-  const int r0 = s * h->ckpt_K;
-  const int r1 = std::min((int)h->store_steps.size(), r0 + h->ckpt_K);
   Wave w{h->d_state2, h->d_v2, h->d_it2, false, false};
-  int r = r0;
-  for (int it = it0 + 1; r < r1; ++it) {
+  int r = rA;
+  for (int it = it0 + 1; r < rB; ++it) {
     float *rec = nullptr;
     int mode = 0;
     if (it == h->store_steps[r]) {
-      rec = h->segbuf[r - r0];
+      rec = h->segbuf[r - rA];
       mode = 1;
       ++r;
     }
     int rc = launch_iteration(h, w, mode, rec);
     if (rc) return rc;
   }
+  return SES3D_OK;
+}
+
+// One level: recomputes the records of segment s (records s K .. min((s+1) K, nrec) - 1)
+// into segbuf by a forward run from checkpoint s on the second wavefield.
+int recompute_segment(ses3d_gpu *h, int s) {
+  Range range_("ses3d recompute segment");
+  int rc = load_wave2(h, h->ckpts[s], h->ckpt_it[s]);
+  if (rc) return rc;
+  const int r0 = s * h->ckpt_K;
+  const int r1 = std::min((int)h->store_steps.size(), r0 + h->ckpt_K);
+  rc = recompute_records(h, h->ckpt_it[s], r0, r1);
+  if (rc) return rc;
   h->seg_loaded = s;
+  return SES3D_OK;
+}
+
+// Two levels, first pass: runs segment s forward from its checkpoint and keeps a full-state
+// checkpoint before the first record of each of its sub-segments 1, 2, ... (sub-segment 0
+// starts at the segment's own checkpoint).
+int recompute_level2(ses3d_gpu *h, int s) {
+  Range range_("ses3d recompute checkpoints");
+  const int r0 = s * h->ckpt_K;
+  const int r1 = std::min((int)h->store_steps.size(), r0 + h->ckpt_K);
+  const int nsub = (r1 - r0 + h->ckpt_K2 - 1) / h->ckpt_K2;
+  const size_t ns = (size_t)h->cfg.n_events * NSTATE * h->geo.N;
+  const size_t nv = (size_t)h->cfg.n_events * 3 * h->geo.G;
+  while ((int)h->ckpt2.size() < nsub - 1) {
+    float *c = nullptr;
+    CK(h, dalloc(&c, ckpt_floats(h)));
+    h->ckpt2.push_back(c);
+  }
+  h->ckpt2_it.assign(std::max(0, nsub - 1), 0);
+  int rc = load_wave2(h, h->ckpts[s], h->ckpt_it[s]);
+  if (rc) return rc;
+  Wave w{h->d_state2, h->d_v2, h->d_it2, false, false};
+  int it = h->ckpt_it[s];
+  for (int j = 1; j < nsub; ++j) {
+    const int target = h->store_steps[r0 + j * h->ckpt_K2] - 1;  // completed iterations at the checkpoint
+    for (; it < target; ++it) {
+      rc = launch_iteration(h, w, 0, nullptr);
+      if (rc) return rc;
+    }
+    CK(h, cudaMemcpyAsync(h->ckpt2[j - 1], h->d_state2, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+    CK(h, cudaMemcpyAsync(h->ckpt2[j - 1] + ns, h->d_v2, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+    h->ckpt2_it[j - 1] = target;
+  }
+  h->seg_loaded = s;
+  h->sub_loaded = -1;
+  return SES3D_OK;
+}
+
+// The forward record r for the adjoint run, recomputed as the checkpointing asks.
+int checkpointed_record(ses3d_gpu *h, int r, float **out) {
+  const int s = r / h->ckpt_K;
+  if (s >= (int)h->ckpts.size()) return fail(h, SES3D_E_STATE, "no checkpoint for this record");
+  if (h->ckpt_K2 <= 0) {
+    if (h->seg_loaded != s) {
+      int rc = recompute_segment(h, s);
+      if (rc) return rc;
+    }
+    *out = h->segbuf[r - s * h->ckpt_K];
+    return SES3D_OK;
+  }
+  if (h->seg_loaded != s) {
+    int rc = recompute_level2(h, s);
+    if (rc) return rc;
+  }
+  const int r0 = s * h->ckpt_K;
+  const int j = (r - r0) / h->ckpt_K2;
+  if (h->sub_loaded != j) {
+    Range range_("ses3d recompute segment");
+    const int rA = r0 + j * h->ckpt_K2;
+    const int rB = std::min({(int)h->store_steps.size(), r0 + h->ckpt_K, rA + h->ckpt_K2});
+    const float *src = j == 0 ? h->ckpts[s] : h->ckpt2[j - 1];
+    const int it0 = j == 0 ? h->ckpt_it[s] : h->ckpt2_it[j - 1];
+    int rc = load_wave2(h, src, it0);
+    if (!rc) rc = recompute_records(h, it0, rA, rB);
+    if (rc) return rc;
+    h->sub_loaded = j;
+  }
+  *out = h->segbuf[r - r0 - j * h->ckpt_K2];
   return SES3D_OK;
 }
 
@@ -513,6 +649,7 @@ int build_graph(ses3d_gpu *h, int len) {
 // run correlates one (ses3d_main.f90:168); every other iteration is plain.
 bool special_iteration(const ses3d_gpu *h, int it) {
   const int nt = h->cfg.nt;
+  if (h->mode_flag == 0) return h->ex_K > 0 && (it - 1) % h->ex_K == 0;  // exact-adjoint checkpoint
   if (h->mode_flag == 1) return it % h->cfg.samp_ad == 0 || it == 1 || it == nt;
   if (h->mode_flag == 2) return h->saving_vector[nt + 1 - it] > 0 && h->record_cursor > 0;
   return false;
@@ -699,6 +836,15 @@ int ses3d_gpu_destroy(ses3d_gpu *h) {
   for (float *r : h->record_blocks) dfree(r);
   for (float *r : h->ckpts) dfree(r);
   for (float *r : h->segbuf) dfree(r);
+  for (float *r : h->ckpt2) dfree(r);
+  for (float *r : h->ex_ckpts) dfree(r);
+  for (float *r : h->ex_slots) dfree(r);
+  for (float *r : h->ex_ckpts2) dfree(r);
+  free_forces(h->fseis);
+  {
+    void *ex[] = {h->d_astate, h->d_av, h->d_aF, h->d_af, h->d_egmat, h->d_egimm, h->d_ait};
+    for (void *q : ex) dfree(q);
+  }
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return SES3D_OK;
@@ -850,10 +996,11 @@ int ses3d_gpu_step(ses3d_gpu *h, int n) {
     const int flag = h->mode_flag;
     // plain iterations replay from a CUDA graph: runs of graph_n in plain forward runs, and
     // in record / adjoint runs the stretches of samp_ad - 1 between stored iterations
-    const int L = flag == 0 ? h->graph_n : std::min(h->graph_n, h->cfg.samp_ad - 1);
+    const int L = flag == 0 ? (h->ex_K > 0 ? std::min(h->graph_n, h->ex_K - 1) : h->graph_n)
+                            : std::min(h->graph_n, h->cfg.samp_ad - 1);
     if (h->graph_on && L > 0 && n - done >= L && nt - h->it >= L) {
       bool plain = true;
-      for (int q = 1; flag != 0 && q <= L && plain; ++q) plain = !special_iteration(h, h->it + q);
+      for (int q = 1; (flag != 0 || h->ex_K > 0) && q <= L && plain; ++q) plain = !special_iteration(h, h->it + q);
       if (plain) {
         if (h->graph_dirty || !h->graph_exec || h->graph_len != L) {
           int rc = build_graph(h, L);
@@ -868,6 +1015,10 @@ int ses3d_gpu_step(ses3d_gpu *h, int n) {
     }
     int mode = 0;
     float *rec = nullptr;
+    if (flag == 0 && h->ex_K > 0 && (it - 1) % h->ex_K == 0) {
+      int rc = save_exact_checkpoint(h, it - 1);
+      if (rc) return rc;
+    }
     if (flag == 1 && (it % h->cfg.samp_ad == 0 || it == 1 || it == nt)) {
       if (h->ckpt_K > 0) {  // checkpoint before every ckpt_K-th record, no records kept
         if (h->nrec_done % h->ckpt_K == 0) {
@@ -897,13 +1048,8 @@ int ses3d_gpu_step(ses3d_gpu *h, int n) {
     } else if (flag == 2 && h->saving_vector[nt + 1 - it] > 0 && h->record_cursor > 0) {
       const int r = --h->record_cursor;
       if (h->ckpt_K > 0) {
-        const int s = r / h->ckpt_K;
-        if (s >= (int)h->ckpts.size()) return fail(h, SES3D_E_STATE, "no checkpoint for this record");
-        if (h->seg_loaded != s) {
-          int rc = recompute_segment(h, s);
-          if (rc) return rc;
-        }
-        rec = h->segbuf[r - s * h->ckpt_K];
+        int rc = checkpointed_record(h, r, &rec);
+        if (rc) return rc;
       } else {
         rec = h->records[r];
       }
@@ -952,7 +1098,9 @@ static int state_field_index(int field) {
   return -1;
 }
 
-static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float *hin) {
+// One field of one event, from / into the handle's wavefield or (adjoint) the exact
+// adjoint's state.
+static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float *hin, bool adjoint = false) {
   int rc = check_event(h, event);
   if (rc) return rc;
   if (field < 0 || field >= SES3D_FIELD_COUNT) return fail(h, SES3D_E_CONFIG, "unknown field");
@@ -962,8 +1110,8 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
     return fail(h, SES3D_E_STATE,
                 "lean iterations did not integrate this displacement gradient outside the PML (set_lean)");
   const long long N = h->geo.N, G = h->geo.G;
-  float *vbase = h->d_v + (size_t)event * 3 * G;
-  float *sbase = h->d_state + (size_t)event * NSTATE * N;
+  float *vbase = (adjoint ? h->d_av : h->d_v) + (size_t)event * 3 * G;
+  float *sbase = (adjoint ? h->d_astate : h->d_state) + (size_t)event * NSTATE * N;
   if (field >= SES3D_FIELD_VX_GLOBAL && field <= SES3D_FIELD_VZ_GLOBAL) {
     float *d = vbase + (size_t)(field - SES3D_FIELD_VX_GLOBAL) * G;
     if (hout) CK(h, cudaMemcpy(hout, d, G * sizeof(float), cudaMemcpyDeviceToHost));
@@ -988,7 +1136,8 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
     if (e != cudaSuccess) return done(cuda_fail(h, e, "copy"));
   } else if (state_field_index(field) >= 0) {
     const int f = state_field_index(field);
-    if (int r = sync_mirrors(h)) return done(r);
+    if (!adjoint)
+      if (int r = sync_mirrors(h)) return done(r);
     cudaError_t e;
     if (hout) {
       e = launch_state_field(sbase, f, tmp, h->geo.E, 1, h->st);
@@ -996,7 +1145,7 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
     } else {
       e = cudaMemcpyAsync(tmp, hin, N * sizeof(float), cudaMemcpyHostToDevice, h->st);
       if (e == cudaSuccess) e = launch_state_field(sbase, f, tmp, h->geo.E, 0, h->st);
-      if (e == cudaSuccess && field >= SES3D_FIELD_DXUX && field <= SES3D_FIELD_DZUY)
+      if (e == cudaSuccess && !adjoint && field >= SES3D_FIELD_DXUX && field <= SES3D_FIELD_DZUY)
         h->du_stale &= ~(1u << (field - SES3D_FIELD_DXUX));
     }
     if (e != cudaSuccess) return done(cuda_fail(h, e, "field transfer"));
@@ -1195,6 +1344,7 @@ int ses3d_gpu_begin_adjoint(ses3d_gpu *h) {
   CK(h, cudaMemsetAsync(h->d_grad, 0, (size_t)h->cfg.n_events * NGRAD * h->geo.N * sizeof(double), h->st));
   h->record_cursor = h->ckpt_K > 0 ? h->nrec_done : (int)h->records.size();
   h->seg_loaded = -1;
+  h->sub_loaded = -1;
   destroy_graph(h);
   int rc = zero_wavefield(h);
   if (rc) return rc;
@@ -1333,10 +1483,18 @@ int ses3d_gpu_use_graph(ses3d_gpu *h, int enable, int n_per_graph) {
 }
 
 int ses3d_gpu_set_checkpointing(ses3d_gpu *h, int records_per_segment) {
+  return ses3d_gpu_set_checkpoint_levels(h, records_per_segment, 0);
+}
+
+int ses3d_gpu_set_checkpoint_levels(ses3d_gpu *h, int records_per_segment, int records_per_subsegment) {
   if (!h) return SES3D_E_CONFIG;
-  if (records_per_segment < 0) return fail(h, SES3D_E_CONFIG, "records_per_segment must be >= 0");
+  if (records_per_segment < 0 || records_per_subsegment < 0)
+    return fail(h, SES3D_E_CONFIG, "records per segment and sub-segment must be >= 0");
+  if (records_per_subsegment > 0 && (records_per_segment == 0 || records_per_subsegment >= records_per_segment))
+    return fail(h, SES3D_E_CONFIG, "records per sub-segment must lie between 1 and records per segment - 1");
   if (h->it != 0 || h->mode_flag != 1) return fail(h, SES3D_E_STATE, "set checkpointing before a flag-1 run starts");
   h->ckpt_K = records_per_segment;
+  h->ckpt_K2 = records_per_subsegment;
   return SES3D_OK;
 }
 
@@ -1350,6 +1508,11 @@ int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
   bytes += std::max(h->records.size(), h->record_slots.size()) * nev * NREC * N * sizeof(float);
   bytes += h->ckpts.size() * ckpt_floats(h) * sizeof(float);
   bytes += h->segbuf.size() * nev * NREC * N * sizeof(float);
+  bytes += h->ckpt2.size() * ckpt_floats(h) * sizeof(float);
+  bytes += h->ex_ckpts.size() * ckpt_floats(h) * sizeof(float);
+  bytes += h->ex_slots.size() * nev * ((size_t)NSTATE * N + 6 * G) * sizeof(float);
+  bytes += h->ex_ckpts2.size() * ckpt_floats(h) * sizeof(float);
+  if (h->d_astate) bytes += nev * (((size_t)NSTATE * N + 6 * G + 3 * N) * sizeof(float) + ((size_t)NMAT * N + G) * sizeof(double));
   if (h->d_state2) bytes += nev * ((size_t)NSTATE * N + 3 * G) * sizeof(float);
   bytes += (size_t)3 * h->cfg.nt * h->R * sizeof(float);
   return (int64_t)bytes;
@@ -1358,6 +1521,8 @@ int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
 int ses3d_gpu_set_lean(ses3d_gpu *h, int enable) {
   if (!h) return SES3D_E_CONFIG;
   if (enable && h->mode_flag != 0) return fail(h, SES3D_E_CONFIG, "lean stepping applies to plain forward runs only");
+  if (enable && h->ex_K > 0)
+    return fail(h, SES3D_E_CONFIG, "the exact adjoint replays full-state iterations; lean stepping is off for it");
   if (!enable) {
     int rc = sync_mirrors(h);
     if (rc) return rc;
@@ -1383,6 +1548,20 @@ int ses3d_gpu_kernel_time(const ses3d_gpu *h, int which, double *total_ms, int64
   return SES3D_OK;
 }
 
+int ses3d_gpu_set_kernel_shape(ses3d_gpu *h, int element_shape, int node_block) {
+  if (!h) return SES3D_E_CONFIG;
+  if (element_shape < 0 || element_shape >= element_shape_count())
+    return fail(h, SES3D_E_CONFIG, "element_shape must be 0 .. " + std::to_string(element_shape_count() - 1));
+  if (node_block != 128 && node_block != 256 && node_block != 512)
+    return fail(h, SES3D_E_CONFIG, "node_block must be 128, 256 or 512");
+  h->shape = element_shape;
+  h->node_block = node_block;
+  destroy_graph(h);
+  return SES3D_OK;
+}
+
+int ses3d_gpu_kernel_shape_count(void) { return element_shape_count(); }
+
 int ses3d_gpu_set_block_elements(ses3d_gpu *h, int elements_per_cta) {
   if (!h) return SES3D_E_CONFIG;
   if (elements_per_cta == 0) elements_per_cta = 1;
@@ -1391,6 +1570,238 @@ int ses3d_gpu_set_block_elements(ses3d_gpu *h, int elements_per_cta) {
   h->epb = elements_per_cta;
   destroy_graph(h);
   return SES3D_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Exact discrete adjoint
+// ---------------------------------------------------------------------------------------
+int ses3d_gpu_exact_adjoint(ses3d_gpu *h, int steps_per_checkpoint, int steps_per_subsegment) {
+  if (!h) return SES3D_E_CONFIG;
+  if (h->mode_flag != 0)
+    return fail(h, SES3D_E_CONFIG, "the exact adjoint differentiates plain forward runs (adjoint_flag 0)");
+  if (steps_per_checkpoint < 1) return fail(h, SES3D_E_CONFIG, "steps_per_checkpoint must be >= 1");
+  if (steps_per_subsegment < 0 || (steps_per_subsegment > 0 && steps_per_subsegment >= steps_per_checkpoint))
+    return fail(h, SES3D_E_CONFIG, "steps_per_subsegment must be 0 or between 1 and steps_per_checkpoint - 1");
+  if (h->it != 0 || h->external_stepped)
+    return fail(h, SES3D_E_STATE, "enable the exact adjoint before the forward run starts");
+  if (h->c.lean) return fail(h, SES3D_E_CONFIG, "switch lean stepping off before enabling the exact adjoint");
+  const size_t nev = h->cfg.n_events, N = h->geo.N, G = h->geo.G;
+  if (!h->d_astate) {
+    CK(h, dalloc(&h->d_astate, nev * NSTATE * N));
+    CK(h, dalloc(&h->d_av, nev * 3 * G));
+    CK(h, dalloc(&h->d_aF, nev * 3 * G));
+    CK(h, dalloc(&h->d_af, nev * 3 * N));
+    CK(h, dalloc(&h->d_egmat, nev * NMAT * N));
+    CK(h, dalloc(&h->d_egimm, nev * G));
+    CK(h, dalloc(&h->d_ait, 1));
+  }
+  CK(h, cudaMemsetAsync(h->d_astate, 0, nev * NSTATE * N * sizeof(float), h->st));
+  CK(h, cudaMemsetAsync(h->d_av, 0, nev * 3 * G * sizeof(float), h->st));
+  CK(h, cudaStreamSynchronize(h->st));
+  h->ex_K = steps_per_checkpoint;
+  h->ex_K2 = steps_per_subsegment;
+  h->seis_adj.assign(nev, std::vector<float>());
+  h->ex_done = false;
+  destroy_graph(h);
+  return SES3D_OK;
+}
+
+int ses3d_gpu_exact_set_seismogram_adjoint(ses3d_gpu *h, int event, const float *gx, const float *gy, const float *gz) {
+  int rc = check_event(h, event);
+  if (rc) return rc;
+  if (h->ex_K <= 0) return fail(h, SES3D_E_STATE, "enable the exact adjoint first (ses3d_gpu_exact_adjoint)");
+  const int nr = h->rec_off[event + 1] - h->rec_off[event], nt = h->cfg.nt;
+  std::vector<float> &g = h->seis_adj[event];
+  g.assign((size_t)3 * nt * nr, 0.f);
+  const float *src[3] = {gx, gy, gz};
+  for (int c = 0; c < 3; ++c)
+    if (src[c]) std::memcpy(g.data() + (size_t)c * nt * nr, src[c], (size_t)nt * nr * sizeof(float));
+  return SES3D_OK;
+}
+
+// The receivers' adjoint sources as point forces on the element contributions to the
+// adjoint velocity: one group per (event, element), receivers in order, weights the
+// receivers' Lagrange weights, time functions -d misfit / d seismogram (k_inject subtracts).
+static int build_seismogram_forces(ses3d_gpu *h) {
+  const int nt = h->cfg.nt;
+  std::map<std::pair<int, long long>, std::vector<int>> groups;
+  std::vector<const Receiver *> recs;
+  std::vector<const float *> series;  // [3][nt][nr] of the receiver's event
+  std::vector<int> rloc, nrs;
+  for (int e = 0; e < h->cfg.n_events; ++e) {
+    const int nr = (int)h->ev[e].recs.size();
+    for (int r = 0; r < nr; ++r) {
+      const Receiver &R = h->ev[e].recs[r];
+      const long long el = R.rx + (long long)h->geo.ex * (R.ry + (long long)h->geo.ey * R.rz);
+      groups[{e, el}].push_back((int)recs.size());
+      recs.push_back(&R);
+      series.push_back(h->seis_adj[e].empty() ? nullptr : h->seis_adj[e].data());
+      rloc.push_back(r);
+      nrs.push_back(nr);
+    }
+  }
+  std::vector<int4> gr;
+  std::vector<float> delta, stf;
+  std::vector<int> mask;
+  int k = 0;
+  for (auto &kv : groups) {
+    int4 g4;
+    g4.x = kv.first.first; g4.y = (int)kv.first.second; g4.z = k;
+    for (int q : kv.second) {
+      delta.insert(delta.end(), recs[q]->weight, recs[q]->weight + NPE);
+      for (int c = 0; c < 3; ++c)
+        for (int t = 0; t < nt; ++t)
+          stf.push_back(series[q] ? -series[q][((size_t)c * nt + t) * nrs[q] + rloc[q]] : 0.f);
+      mask.push_back(7);
+      ++k;
+    }
+    g4.w = k;
+    gr.push_back(g4);
+  }
+  ForceSet &F = h->fseis;
+  free_forces(F);
+  F.n = (int)gr.size();
+  if (F.n) {
+    CK(h, dalloc(&F.groups, gr.size()));
+    CK(h, dalloc(&F.delta, delta.size()));
+    CK(h, dalloc(&F.stf, stf.size()));
+    CK(h, dalloc(&F.mask, mask.size()));
+    CK(h, cudaMemcpy(F.groups, gr.data(), gr.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(F.delta, delta.data(), delta.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(F.stf, stf.data(), stf.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(F.mask, mask.data(), mask.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  return SES3D_OK;
+}
+
+int ses3d_gpu_exact_backward(ses3d_gpu *h) {
+  Range range_("ses3d exact backward");
+  if (!h) return SES3D_E_CONFIG;
+  if (h->ex_K <= 0) return fail(h, SES3D_E_STATE, "enable the exact adjoint before the forward run");
+  const int nt = h->cfg.nt, K = h->ex_K;
+  if (h->it != nt) return fail(h, SES3D_E_STATE, "the forward run must be complete (nt iterations)");
+  if (h->ex_done) return fail(h, SES3D_E_STATE, "the backward run of this forward run is done");
+  const int nseg = (nt + K - 1) / K;
+  if ((int)h->ex_ckpts.size() < nseg) return fail(h, SES3D_E_STATE, "missing exact-adjoint checkpoints");
+  int rc = build_seismogram_forces(h);
+  if (rc) return rc;
+  const size_t nev = h->cfg.n_events, N = h->geo.N, G = h->geo.G;
+  const size_t ns = nev * NSTATE * N, nv = nev * 3 * G;
+  CK(h, cudaMemsetAsync(h->d_egmat, 0, nev * NMAT * N * sizeof(double), h->st));
+  CK(h, cudaMemsetAsync(h->d_egimm, 0, nev * G * sizeof(double), h->st));
+  const int ait0 = nt - 1;
+  CK(h, cudaMemcpyAsync(h->d_ait, &ait0, sizeof(int), cudaMemcpyHostToDevice, h->st));
+  const int K2 = h->ex_K2 > 0 ? h->ex_K2 : K;  // iterations recomputed into slots at a time
+  while ((int)h->ex_slots.size() < std::min(K2, nt)) {
+    float *q = nullptr;
+    CK(h, dalloc(&q, ns + 2 * nv));
+    h->ex_slots.push_back(q);
+  }
+  const int nsub_max = (std::min(K, nt) + K2 - 1) / K2;
+  while ((int)h->ex_ckpts2.size() < nsub_max - 1) {
+    float *q = nullptr;
+    CK(h, dalloc(&q, ckpt_floats(h)));
+    h->ex_ckpts2.push_back(q);
+  }
+  Ptrs p = make_ptrs(h);
+  AdjPtrs a;
+  std::memset(&a, 0, sizeof(a));
+  a.astate = h->d_astate; a.av = h->d_av; a.aF = h->d_aF; a.af = h->d_af;
+  a.gmat = h->d_egmat; a.gimm = h->d_egimm; a.d_ait = h->d_ait;
+  rc = ensure_wave2(h);  // the recomputing wavefield must exist before its pointers are taken
+  if (rc) return rc;
+  const Wave w{h->d_state2, h->d_v2, h->d_it2, false, false};
+  for (int sg = nseg - 1; sg >= 0; --sg) {
+    const int t0 = sg * K, t1 = std::min(t0 + K, nt);
+    const int nsub = (t1 - t0 + K2 - 1) / K2;
+    if (nsub > 1) {  // second level: checkpoints before sub-segments 1 .. nsub - 1 of the segment
+      Range r2("ses3d exact recompute checkpoints");
+      rc = load_wave2(h, h->ex_ckpts[sg], t0);
+      if (rc) return rc;
+      int t = t0;
+      for (int j = 1; j < nsub; ++j) {
+        for (; t < t0 + j * K2; ++t) {
+          rc = launch_iteration(h, w, 0, nullptr);
+          if (rc) return rc;
+        }
+        CK(h, cudaMemcpyAsync(h->ex_ckpts2[j - 1], h->d_state2, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+        CK(h, cudaMemcpyAsync(h->ex_ckpts2[j - 1] + ns, h->d_v2, nv * sizeof(float), cudaMemcpyDeviceToDevice,
+                              h->st));
+      }
+    }
+    for (int j = nsub - 1; j >= 0; --j) {
+      const int a0 = t0 + j * K2, a1 = std::min(a0 + K2, t1);
+      {  // forward recompute of the sub-segment, keeping the state before each iteration and its forces
+        Range r2("ses3d exact recompute");
+        rc = load_wave2(h, j == 0 ? h->ex_ckpts[sg] : h->ex_ckpts2[j - 1], a0);
+        if (rc) return rc;
+        for (int t = a0 + 1; t <= a1; ++t) {
+          float *slot = h->ex_slots[t - a0 - 1];
+          CK(h, cudaMemcpyAsync(slot, h->d_state2, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+          CK(h, cudaMemcpyAsync(slot + ns, h->d_v2, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+          rc = launch_iteration(h, w, 0, nullptr, false, slot + ns + nv);
+          if (rc) return rc;
+        }
+      }
+      for (int t = a1; t > a0; --t) {  // backward iterations a1 .. a0 + 1
+        const float *slot = h->ex_slots[t - a0 - 1];
+        a.fstate = slot; a.fv = slot + ns; a.fg = slot + ns + nv;
+        CK(h, launch_adjoint_node1(h->c, p, a, h->st));
+        CK(h, launch_adjoint_element(h->cfg.is_diss, h->c, p, a, h->st));
+        if (h->fseis.n)
+          CK(h, launch_inject(h->c, h->d_af, h->fseis.groups, h->fseis.n, h->fseis.delta, h->fseis.stf,
+                              h->fseis.mask, h->d_ait, h->st));
+        CK(h, launch_adjoint_node2(h->c, a, h->st));
+        h->launches += h->fseis.n ? 4 : 3;
+      }
+    }
+  }
+  CK(h, cudaStreamSynchronize(h->st));
+  rc = check_device_error(h);
+  if (rc) return rc;
+  h->ex_done = true;
+  return SES3D_OK;
+}
+
+int ses3d_gpu_exact_gradient(ses3d_gpu *h, int which, double *out, int device) {
+  if (!h) return SES3D_E_CONFIG;
+  if (which < 0 || which > 6 || !out) return fail(h, SES3D_E_CONFIG, "which must be 0..6 (rhoinv, mu, lambda, A, B, C, Q)");
+  if (!h->ex_done) return fail(h, SES3D_E_STATE, "run ses3d_gpu_exact_backward first");
+  if (which == 6 && !h->cfg.is_diss) return fail(h, SES3D_E_CONFIG, "Q is a model record only with attenuation");
+  const long long N = h->geo.N;
+  double *dst = out, *tmp = nullptr;
+  if (!device) {
+    CK(h, dalloc(&tmp, (size_t)N));
+    dst = tmp;
+  }
+  float sD = h->cfg.D_p[0];
+  sD = sD + h->cfg.D_p[1];
+  sD = sD + h->cfg.D_p[2];
+  Ptrs p = make_ptrs(h);
+  cudaError_t e = launch_adjoint_model_gradient(h->c, p, h->d_egmat, h->d_egimm, which, h->cfg.is_diss, (double)sD,
+                                                h->d_tab + h->o_z, h->d_tab + h->o_sin, h->d_tab + h->o_w, dst, h->st);
+  if (e == cudaSuccess && !device) e = cudaMemcpyAsync(out, tmp, N * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  dfree(tmp);
+  if (e != cudaSuccess) return cuda_fail(h, e, "exact_gradient");
+  ++h->launches;
+  return SES3D_OK;
+}
+
+int ses3d_gpu_exact_get_field(ses3d_gpu *h, int event, int field, float *out) {
+  if (!h) return SES3D_E_CONFIG;
+  if (!out) return fail(h, SES3D_E_CONFIG, "null output");
+  if (!h->d_astate) return fail(h, SES3D_E_STATE, "enable the exact adjoint first (ses3d_gpu_exact_adjoint)");
+  if (field == SES3D_FIELD_MM_GLOBAL) return fail(h, SES3D_E_CONFIG, "MM_global is not part of the adjoint state");
+  return field_io(h, event, field, out, nullptr, true);
+}
+
+int ses3d_gpu_exact_set_field(ses3d_gpu *h, int event, int field, const float *in) {
+  if (!h) return SES3D_E_CONFIG;
+  if (!in) return fail(h, SES3D_E_CONFIG, "null input");
+  if (!h->d_astate) return fail(h, SES3D_E_STATE, "enable the exact adjoint first (ses3d_gpu_exact_adjoint)");
+  if (field == SES3D_FIELD_MM_GLOBAL) return fail(h, SES3D_E_CONFIG, "MM_global is not part of the adjoint state");
+  return field_io(h, event, field, nullptr, in, true);
 }
 
 }  // extern "C"
@@ -1451,14 +1862,14 @@ extern "C" int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int
       CK(h, launch_receivers(h->c, v, h->d_rec_elem, h->d_rec_ev, h->d_rec_w, h->d_seis, h->R, h->d_it, h->st));
       ++h->launches;
     }
-    CK(h, launch_element(h->cfg.is_diss, 0, h->epb, h->c, p, h->st));
+    CK(h, launch_element(h->cfg.is_diss, 0, h->epb, h->shape, h->c, p, h->st));
     ++h->launches;
     if (h->fset[0].n) {
       const ForceSet &F = h->fset[0];
       CK(h, launch_inject(h->c, forces, F.groups, F.n, F.delta, F.stf, F.mask, h->d_it, h->st));
       ++h->launches;
     }
-    CK(h, launch_node(h->c, p, h->st));
+    CK(h, launch_node(h->node_block, h->c, p, h->st));
     ++h->launches;
     h->it += 1;
   }

@@ -14,6 +14,7 @@
 // node-centric gather of k_node: each global node sums its (up to 8) element
 // contributions in the reference loop order, without atomics, so runs are bit-reproducible.
 #include "kernels.cuh"
+#include "assembly.cuh"
 
 // Minimum resident CTAs per SM requested from ptxas for k_element (register cap).
 #ifndef SES3D_ELEM_MINB
@@ -564,8 +565,10 @@ __device__ __forceinline__ void gather_v_async(const Consts &c, const Ptrs &p, l
   asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
-template <bool DISS, int MODE>
-__global__ void __launch_bounds__(TPE, SES3D_TMA_MINB) k_element_tma(const Consts c, const Ptrs p) {
+// MINB: resident CTAs per SM requested from ptxas (register cap); REFILL: when the next
+// item's bulk copy is issued (0: the measured rule below, 1: the other point).
+template <bool DISS, int MODE, int MINB = SES3D_TMA_MINB, int REFILL = 0>
+__global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const Ptrs p) {
   extern __shared__ __align__(128) unsigned char smem[];
   ElemStage *stage = reinterpret_cast<ElemStage *>(smem);
   float (*s_vb)[TPE] = reinterpret_cast<float (*)[TPE]>(smem + TMA_STAGES * sizeof(ElemStage));  // [TMA_VBUF][3]
@@ -665,7 +668,7 @@ __global__ void __launch_bounds__(TPE, SES3D_TMA_MINB) k_element_tma(const Const
     // short, so right after this item's state has been read; full-state items after the
     // stress/divergence barrier, which keeps thread 0's copy work off that barrier
     // (2.65 -> 2.42 ms per launch), while lean iterations lose 6 % that way.
-    constexpr bool LATE_REFILL = MODE != 3;
+    constexpr bool LATE_REFILL = (MODE != 3) != (REFILL == 1);
     if (!LATE_REFILL) issue_refill();
     const size_t m0 = (size_t)e * 125 + nn;
     float *S = p.state + ((size_t)ev * c.E + e) * ELEM_STATE + nn;
@@ -682,16 +685,18 @@ __global__ void __launch_bounds__(TPE, SES3D_TMA_MINB) k_element_tma(const Const
 // ses3d_evolution.f90:286-310), then a = s / MM, v += dt (a - prof v), v *= taper
 // (ses3d_evolution.f90:318-328,366).
 // ---------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(SES3D_NODE_TPB, SES3D_NODE_MINB) k_node(const Consts c, const Ptrs p) {
+// STORE_F: also write the assembled forces (a run whose states the exact adjoint replays).
+// TPB threads per CTA, MINB resident CTAs per SM requested from ptxas.
+template <bool STORE_F, int TPB = SES3D_NODE_TPB, int MINB = SES3D_NODE_MINB>
+__global__ void __launch_bounds__(TPB, MINB) k_node(const Consts c, const Ptrs p) {
   const int gz = blockIdx.y, ev = blockIdx.z;
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
     *p.d_it += 1;  // every reader of the counter ran earlier in stream order
   const unsigned GXY = (unsigned)c.GX * (unsigned)c.GY;
-  const unsigned t = blockIdx.x * (unsigned)SES3D_NODE_TPB + threadIdx.x;
+  const unsigned t = blockIdx.x * (unsigned)TPB + threadIdx.x;
   if (t >= GXY) return;
 #if SES3D_NODE_MAGIC
-  const unsigned hi = __umulhi(t, c.gx_magic);
-  const int gy = (int)((hi + ((t - hi) >> 1)) >> c.gx_shift);
+  const int gy = node_row(c, t);
 #else
   const int gy = (int)(t / (unsigned)c.GX);
 #endif
@@ -702,68 +707,16 @@ __global__ void __launch_bounds__(SES3D_NODE_TPB, SES3D_NODE_MINB) k_node(const 
   float vx = V[0], vy = V[c.G], vz = V[2 * c.G];
   const float imm = __ldg(p.iMM + g);
   const float pxr = __ldg(p.pxg + gx), pyr = __ldg(p.pyg + gy), pzr = __ldg(p.pzg + gz);
-  const int i0 = gx == 0 ? 0 : (gx - 1) >> 2, i1 = min(gx >> 2, c.ex - 1);
-  const int j0 = gy == 0 ? 0 : (gy - 1) >> 2, j1 = min(gy >> 2, c.ey - 1);
-  const int k0 = gz == 0 ? 0 : (gz - 1) >> 2, k1 = min(gz >> 2, c.ez - 1);
-  const float *F = p.f + (size_t)ev * 3 * (size_t)c.N;  // 3 N < 2^32 is checked at create
-  // Contributions (i, j, k) in {i0, i1} x {j0, j1} x {k0, k1}, summed in the reference
-  // order (i, then j, then k ascending). Whether a node lies on a y or z element face is
-  // the same for a warp of consecutive gx (one gy row), so the four cases below do not
-  // diverge; the x face (every fourth gx) is predicated. At most four contributions are
-  // in flight at a time.
-  const unsigned sy_ = (unsigned)c.ex * 375u, sz_ = sy_ * (unsigned)c.ey;
-  const unsigned q0 = ((unsigned)i0 * 371u + (unsigned)gx) + ((unsigned)j0 * (sy_ - 20u) + 5u * (unsigned)gy) +
-                      ((unsigned)k0 * (sz_ - 100u) + 25u * (unsigned)gz);
-  const unsigned dx = (unsigned)(i1 - i0) * 371u, dy = (unsigned)(j1 - j0) * (sy_ - 20u),
-                 dz = (unsigned)(k1 - k0) * (sz_ - 100u);
-  const bool ux = i1 != i0, uy = j1 != j0, uz = k1 != k0;
-  float sx = 0.f, sy = 0.f, sz = 0.f;
-  if (!uy && !uz) {
-    const float a0 = F[q0], a1 = F[q0 + 125], a2 = F[q0 + 250];
-    float b0 = 0.f, b1 = 0.f, b2 = 0.f;
-    if (ux) { b0 = F[q0 + dx]; b1 = F[q0 + dx + 125]; b2 = F[q0 + dx + 250]; }
-    sx = 0.f + a0; sy = 0.f + a1; sz = 0.f + a2;
-    if (ux) { sx += b0; sy += b1; sz += b2; }
-  } else if (!uy || !uz) {  // one of the y / z faces: contributions q0, q0 + d (+ the x pair)
-    const unsigned d = uz ? dz : dy;
-    const float a0 = F[q0], a1 = F[q0 + 125], a2 = F[q0 + 250];
-    const float c0 = F[q0 + d], c1 = F[q0 + d + 125], c2 = F[q0 + d + 250];
-    float b0 = 0.f, b1 = 0.f, b2 = 0.f, e0 = 0.f, e1 = 0.f, e2 = 0.f;
-    if (ux) {
-      b0 = F[q0 + dx]; b1 = F[q0 + dx + 125]; b2 = F[q0 + dx + 250];
-      e0 = F[q0 + dx + d]; e1 = F[q0 + dx + d + 125]; e2 = F[q0 + dx + d + 250];
-    }
-    sx = 0.f + a0; sy = 0.f + a1; sz = 0.f + a2;
-    sx += c0; sy += c1; sz += c2;
-    if (ux) { sx += b0; sy += b1; sz += b2; sx += e0; sy += e1; sz += e2; }
-  } else {  // y and z faces: i0 half (4 contributions), then the i1 half
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      if (h == 1 && !ux) break;
-      const unsigned q = q0 + (h ? dx : 0u);
-      const float f00 = F[q], f01 = F[q + 125], f02 = F[q + 250];
-      const float f10 = F[q + dz], f11 = F[q + dz + 125], f12 = F[q + dz + 250];
-      const float f20 = F[q + dy], f21 = F[q + dy + 125], f22 = F[q + dy + 250];
-      const float f30 = F[q + dy + dz], f31 = F[q + dy + dz + 125], f32 = F[q + dy + dz + 250];
-      if (h == 0) { sx = 0.f + f00; sy = 0.f + f01; sz = 0.f + f02; }
-      else { sx += f00; sy += f01; sz += f02; }
-      sx += f10; sy += f11; sz += f12;
-      sx += f20; sy += f21; sz += f22;
-      sx += f30; sy += f31; sz += f32;
-    }
+  float sx, sy, sz;
+  gather_node(c, p.f + (size_t)ev * 3 * (size_t)c.N, gx, gy, gz, sx, sy, sz);
+  if (STORE_F) {
+    float *Fo = p.fg + (size_t)ev * 3 * c.G + g;
+    Fo[0] = sx; Fo[c.G] = sy; Fo[2 * c.G] = sz;
   }
   // a = s / MM with the reciprocal of the mass matrix (ses3d_evolution.f90:318-320)
   const float ax = sx * imm, ay = sy * imm, az = sz * imm;
-  float prof = 0.f, taper = 1.f;
-  const float praw = __fadd_rn(__fadd_rn(pxr, pyr), pzr);
-  if (praw != 0.f) {
-    const float den = __fadd_rn(1.f, __fdiv_rn(praw, 1.2f));
-    const float pz = __fdiv_rn(__fmul_rn(2.f, pzr), den);
-    const float py = __fdiv_rn(__fmul_rn(2.f, pyr), den);
-    const float px = __fdiv_rn(__fmul_rn(2.f, pxr), den);
-    prof = __fadd_rn(__fadd_rn(px, py), pz);
-    taper = expf(-__fmul_rn(__fmul_rn(0.1f, prof), prof));
-  }
+  float px, py, pz, prof, taper;
+  pml_profiles(pxr, pyr, pzr, px, py, pz, prof, taper);
   const float dt = c.dt;
   vx = vx + dt * (ax - prof * vx);
   vy = vy + dt * (ay - prof * vy);
@@ -1073,50 +1026,80 @@ static cudaError_t launch_elem_epb(int epb, const Consts &c, const Ptrs &p, cuda
   }
 }
 
-// Resident CTAs of k_element_tma<DISS, MODE> on the current device (set by prepare_tma).
-template <bool DISS, int MODE>
+// Block shapes of the persistent element kernel selectable at run time (the autotuner's
+// search space): {resident CTAs per SM, refill point}.
+constexpr int kTmaShapes = 4;
+template <int S> struct TmaShape;
+template <> struct TmaShape<0> { static constexpr int minb = 5, refill = 0; };  // measured default
+template <> struct TmaShape<1> { static constexpr int minb = 4, refill = 0; };
+template <> struct TmaShape<2> { static constexpr int minb = 6, refill = 0; };
+template <> struct TmaShape<3> { static constexpr int minb = 5, refill = 1; };
+
+// Resident CTAs of one instantiation of k_element_tma on the current device (set by prepare_tma).
+template <bool DISS, int MODE, int S>
 static int &tma_grid_cap() {
   static int cap = 0;
   return cap;
 }
-template <bool DISS, int MODE>
+template <bool DISS, int MODE, int S>
 static cudaError_t prepare_tma() {
-  cudaError_t e = cudaFuncSetAttribute(k_element_tma<DISS, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)TMA_SMEM);
+  auto kern = k_element_tma<DISS, MODE, TmaShape<S>::minb, TmaShape<S>::refill>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TMA_SMEM);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_element_tma<DISS, MODE>, TPE, TMA_SMEM);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TPE, TMA_SMEM);
   if (e != cudaSuccess) return e;
-  tma_grid_cap<DISS, MODE>() = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  tma_grid_cap<DISS, MODE, S>() = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
   return cudaSuccess;
+}
+template <int S>
+static cudaError_t prepare_tma_shape() {
+  cudaError_t e;
+  if ((e = prepare_tma<false, 0, S>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<false, 3, S>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<true, 0, S>()) != cudaSuccess) return e;
+  return prepare_tma<true, 3, S>();
 }
 // Sets the shared-memory limit and grid size of the persistent element kernels; called
 // when a handle is created, before any stream capture.
 cudaError_t prepare_element_kernels() {
   cudaError_t e;
-  if ((e = prepare_tma<false, 0>()) != cudaSuccess) return e;
-  if ((e = prepare_tma<false, 3>()) != cudaSuccess) return e;
-  if ((e = prepare_tma<true, 0>()) != cudaSuccess) return e;
-  return prepare_tma<true, 3>();
+  if ((e = prepare_tma_shape<0>()) != cudaSuccess) return e;
+  if ((e = prepare_tma_shape<1>()) != cudaSuccess) return e;
+  if ((e = prepare_tma_shape<2>()) != cudaSuccess) return e;
+  return prepare_tma_shape<3>();
 }
 
-template <bool DISS, int MODE>
+template <bool DISS, int MODE, int S>
 static cudaError_t launch_tma(const Consts &c, const Ptrs &p, cudaStream_t st) {
-  const int grid_cap = tma_grid_cap<DISS, MODE>();
+  const int grid_cap = tma_grid_cap<DISS, MODE, S>();
   if (grid_cap <= 0) return cudaErrorInitializationError;
   const long long total = c.E * (long long)c.nev;
   const unsigned blocks = (unsigned)(total < grid_cap ? total : grid_cap);
-  k_element_tma<DISS, MODE><<<blocks, TPE, TMA_SMEM, st>>>(c, p);
+  k_element_tma<DISS, MODE, TmaShape<S>::minb, TmaShape<S>::refill><<<blocks, TPE, TMA_SMEM, st>>>(c, p);
   return cudaGetLastError();
 }
 
-cudaError_t launch_element(int diss, int mode, int epb, const Consts &c, const Ptrs &p, cudaStream_t st) {
+template <bool DISS, int MODE>
+static cudaError_t launch_tma_shape(int shape, const Consts &c, const Ptrs &p, cudaStream_t st) {
+  switch (shape) {
+    case 1: return launch_tma<DISS, MODE, 1>(c, p, st);
+    case 2: return launch_tma<DISS, MODE, 2>(c, p, st);
+    case 3: return launch_tma<DISS, MODE, 3>(c, p, st);
+    default: return launch_tma<DISS, MODE, 0>(c, p, st);
+  }
+}
+
+int element_shape_count() { return kTmaShapes; }
+
+// shape: block shape of the persistent kernel (epb 1); epb 2, 4: register-staged kernel.
+cudaError_t launch_element(int diss, int mode, int epb, int shape, const Consts &c, const Ptrs &p, cudaStream_t st) {
   if (mode == 0 && c.lean) mode = 3;
   if (epb <= 1 && (mode == 0 || mode == 3)) {  // persistent TMA-pipelined kernel
-    if (diss) return mode == 3 ? launch_tma<true, 3>(c, p, st) : launch_tma<true, 0>(c, p, st);
-    return mode == 3 ? launch_tma<false, 3>(c, p, st) : launch_tma<false, 0>(c, p, st);
+    if (diss) return mode == 3 ? launch_tma_shape<true, 3>(shape, c, p, st) : launch_tma_shape<true, 0>(shape, c, p, st);
+    return mode == 3 ? launch_tma_shape<false, 3>(shape, c, p, st) : launch_tma_shape<false, 0>(shape, c, p, st);
   }
   if (diss) {
     if (mode == 1) return launch_elem_epb<true, 1>(epb, c, p, st);
@@ -1130,10 +1113,25 @@ cudaError_t launch_element(int diss, int mode, int epb, const Consts &c, const P
   return launch_elem_epb<false, 0>(epb, c, p, st);
 }
 
-cudaError_t launch_node(const Consts &c, const Ptrs &p, cudaStream_t st) {
-  dim3 grid((unsigned)(((long long)c.GX * c.GY + SES3D_NODE_TPB - 1) / SES3D_NODE_TPB), (unsigned)c.GZ, (unsigned)c.nev);
-  k_node<<<grid, SES3D_NODE_TPB, 0, st>>>(c, p);
+template <bool STORE_F, int TPB, int MINB>
+static cudaError_t launch_node_tpb(const Consts &c, const Ptrs &p, cudaStream_t st) {
+  dim3 grid((unsigned)(((long long)c.GX * c.GY + TPB - 1) / TPB), (unsigned)c.GZ, (unsigned)c.nev);
+  k_node<STORE_F, TPB, MINB><<<grid, TPB, 0, st>>>(c, p);
   return cudaGetLastError();
+}
+
+// node_block: threads per CTA of the node kernel, 128, 256 (default) or 512, each with the
+// resident CTAs per SM that fill 1,536-1,792 thread slots.
+template <bool STORE_F>
+static cudaError_t launch_node_shape(int node_block, const Consts &c, const Ptrs &p, cudaStream_t st) {
+  if (node_block == 128) return launch_node_tpb<STORE_F, 128, 14>(c, p, st);
+  if (node_block == 512) return launch_node_tpb<STORE_F, 512, 3>(c, p, st);
+  return launch_node_tpb<STORE_F, SES3D_NODE_TPB, SES3D_NODE_MINB>(c, p, st);
+}
+
+cudaError_t launch_node(int node_block, const Consts &c, const Ptrs &p, cudaStream_t st) {
+  if (p.fg) return launch_node_shape<true>(node_block, c, p, st);
+  return launch_node_shape<false>(node_block, c, p, st);
 }
 
 cudaError_t launch_receivers(const Consts &c, const float *v, const int *rec_elem, const int *rec_ev,

@@ -73,6 +73,7 @@ struct Ptrs {
   float *state;                         // [nev][E][NSTATE][125]
   float *v;                             // [nev][3][G]
   float *f;                             // [nev][E][3][125] element-local forces (scratch)
+  float *fg;                            // [nev][3][G] assembled forces of the iteration, or null
   int *d_it;                            // completed iterations
   int *err;                             // device error word (bounded waits that gave up)
   // moment-tensor source per event
@@ -84,6 +85,22 @@ struct Ptrs {
   float *rec;                           // record of this iteration: [nev][NREC][N]
   double *grad;                         // [nev][NGRAD][N]
   int grad_q;                           // accumulate the Q kernels too
+};
+
+// Exact discrete adjoint of one iteration (adjoint.cu): the forward state the iteration
+// started from and the forces it assembled, the adjoint state, scratch and the FP64
+// gradient accumulators.
+struct AdjPtrs {
+  const float *fstate;                  // [nev][E][NSTATE][125] forward state before the iteration
+  const float *fv;                      // [nev][3][G] forward velocity before the iteration
+  const float *fg;                      // [nev][3][G] assembled forces of the iteration
+  float *astate;                        // [nev][E][NSTATE][125] adjoint state (in: after, out: before)
+  float *av;                            // [nev][3][G] adjoint velocity (in: after, out: before)
+  float *aF;                            // [nev][3][G] adjoint of the assembled forces (scratch)
+  float *af;                            // [nev][E][3][125] element contributions to the adjoint velocity
+  double *gmat;                         // [nev][E][NMAT][125] d misfit / d stress-rate coefficient
+  double *gimm;                         // [nev][G] d misfit / d (1 / MM)
+  int *d_ait;                           // iteration counter of the backward run (iteration - 1)
 };
 
 }  // namespace ses3d

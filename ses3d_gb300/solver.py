@@ -17,6 +17,8 @@ import numpy as np
 from . import _lib as L
 from . import formats as F
 
+RECORD_NAMES = ("rhoinv", "mu", "lambda", "A", "B", "C", "Q")
+
 
 def config_from(box: F.Box, setup: F.Setup, nt: int, dt, tau, D, pml: int = 2, adjoint_flag: Optional[int] = None,
                 n_events: int = 1, grad_variant: int = 0) -> L.Config:
@@ -64,6 +66,7 @@ class Simulation:
         self.n_events = cfg.n_events
         self._nr = [0] * cfg.n_events
         self._kept = [np.zeros(0, np.int32)] * cfg.n_events
+        self._shape = {"elements_per_cta": 1, "element_shape": 0, "node_block": 256}
 
     # -- construction helpers -------------------------------------------------------------------
     @classmethod
@@ -164,27 +167,63 @@ class Simulation:
 
     def set_block_elements(self, n: int):
         self._check(self.lib.ses3d_gpu_set_block_elements(self.h, int(n)))
+        self._shape["elements_per_cta"] = int(n) or 1
 
-    def autotune(self, steps_each: int = 2, candidates=(1, 2, 4)) -> dict:
-        """Block-shape autotuner: times the element kernel (CUDA events) over `steps_each`
-        real iterations per candidate elements-per-CTA (1 = the persistent bulk-copy kernel,
-        2 and 4 = the register-staged kernel), keeps the fastest and returns
-        {candidate: ms per launch}. The iterations it spends are part of the run (the time
-        axis advances), so call it during warm-up; candidates without steps_each iterations
-        left are skipped."""
-        timings = {}
-        for epb in candidates:
-            if self.nt - self.it < steps_each:
-                break
-            self.set_block_elements(epb)
+    def set_kernel_shape(self, element_shape: int = 0, node_block: int = 256):
+        """Block shapes of the persistent element kernel and the node kernel (ses3d_gpu.h)."""
+        self._check(self.lib.ses3d_gpu_set_kernel_shape(self.h, int(element_shape), int(node_block)))
+        self._shape.update(element_shape=int(element_shape), node_block=int(node_block))
+
+    @property
+    def shape(self) -> dict:
+        return dict(self._shape)
+
+    def autotune(self, steps_each: int = 2, node_blocks=(256, 128, 512)) -> dict:
+        """Block-shape autotuner over the kernels' real shapes: the persistent element kernel
+        in each of its compiled shapes (resident CTAs per SM, refill point) and the
+        register-staged kernel with 2 and 4 elements per CTA, then the node kernel's block
+        sizes. Each candidate runs one untimed iteration (first launch of its instance) and
+        steps_each iterations timed per launch with CUDA events on the library's stream; the
+        fastest is kept. The iterations are part of the run (the time axis advances), so call
+        it during warm-up; it stops early when the run has too few iterations left. Returns
+        {"element": {candidate: ms}, "node": {block: ms}, "chosen": shape}."""
+        n_shapes = int(self.lib.ses3d_gpu_kernel_shape_count())
+        cands = [("persistent", 1, s) for s in range(n_shapes)] + [("register", 2, 0), ("register", 4, 0)]
+        el = {}
+        nodes = {}
+
+        def timed(which):
+            if self.nt - self.it < steps_each + 1:
+                return None
+            self.step(1)
             self.profile(True)
             self.step(steps_each)
-            ms, n = self.kernel_time("element")
-            timings[epb] = ms / max(n, 1)
-        self.profile(False)
-        if timings:
-            self.set_block_elements(min(timings, key=timings.get))
-        return timings
+            ms, n = self.kernel_time(which)
+            self.profile(False)
+            return ms / max(n, 1)
+
+        for kind, epb, shp in cands:
+            self.set_block_elements(epb)
+            self.set_kernel_shape(shp, self._shape["node_block"])
+            t = timed("element")
+            if t is None:
+                break
+            el["%s epb=%d shape=%d" % (kind, epb, shp)] = (t, epb, shp)
+        if el:
+            _, epb, shp = min(el.values(), key=lambda v: v[0])
+            self.set_block_elements(epb)
+            self._shape.update(elements_per_cta=epb, element_shape=shp)
+        for nb in node_blocks:
+            self.set_kernel_shape(self._shape["element_shape"], nb)
+            t = timed("node")
+            if t is None:
+                break
+            nodes[nb] = t
+        if nodes:
+            self._shape["node_block"] = min(nodes, key=nodes.get)
+        self.set_block_elements(self._shape["elements_per_cta"])
+        self.set_kernel_shape(self._shape["element_shape"], self._shape["node_block"])
+        return {"element": {k: v[0] for k, v in el.items()}, "node": nodes, "chosen": self.shape}
 
     def begin_adjoint(self):
         self._check(self.lib.ses3d_gpu_begin_adjoint(self.h))
@@ -281,6 +320,45 @@ class Simulation:
         n = ctypes.c_int64(0)
         self._check(self.lib.ses3d_gpu_kernel_time(self.h, idx, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
+
+    # -- exact discrete adjoint -------------------------------------------------------------------
+    def exact_adjoint(self, steps_per_checkpoint: int, steps_per_subsegment: int = 0):
+        """Plain forward run whose time step is reversed by exact_backward (see ses3d_gpu.h);
+        call before stepping, lean stepping off."""
+        self._check(self.lib.ses3d_gpu_exact_adjoint(self.h, int(steps_per_checkpoint), int(steps_per_subsegment)))
+
+    def set_seismogram_adjoint(self, event: int, gx, gy, gz):
+        """d misfit / d seismogram of one event, each (nr, nt) like seismograms()."""
+        nr = self._nr[event]
+        arrs = [np.ascontiguousarray(np.asarray(g, np.float32).reshape(nr, self.nt).T) for g in (gx, gy, gz)]
+        self._check(self.lib.ses3d_gpu_exact_set_seismogram_adjoint(self.h, event, *[L.fptr(a) for a in arrs]))
+
+    def exact_backward(self):
+        self._check(self.lib.ses3d_gpu_exact_backward(self.h))
+
+    def exact_gradient(self, name: str) -> np.ndarray:
+        """Event-summed d misfit / d model record (rhoinv, mu, lambda, A, B, C, Q), FP64."""
+        out = np.zeros(self.N, np.float64)
+        self._check(self.lib.ses3d_gpu_exact_gradient(self.h, RECORD_NAMES.index(name), L.dptr(out), 0))
+        return out
+
+    def exact_gradient_device(self, name: str, out_ptr: int):
+        """The same, written to N doubles of device memory at out_ptr."""
+        self._check(self.lib.ses3d_gpu_exact_gradient(self.h, RECORD_NAMES.index(name), ctypes.c_void_p(out_ptr), 1))
+
+    def exact_field(self, name: str, event: int = 0) -> np.ndarray:
+        """A field of the exact adjoint's state (after exact_backward: the adjoint of the
+        initial state)."""
+        n = self.G if name.endswith("_global") else (3 * self.N if name.startswith("M") else self.N)
+        out = np.zeros(n, np.float32)
+        self._check(self.lib.ses3d_gpu_exact_get_field(self.h, event, L.FIELD_ID[name], L.fptr(out)))
+        return out
+
+    def set_exact_field(self, name: str, values: np.ndarray, event: int = 0):
+        """Sets a field of the exact adjoint's state (before exact_backward: the adjoint of the
+        final state)."""
+        a = np.ascontiguousarray(values, np.float32)
+        self._check(self.lib.ses3d_gpu_exact_set_field(self.h, event, L.FIELD_ID[name], L.fptr(a)))
 
     @property
     def launch_count(self) -> int:

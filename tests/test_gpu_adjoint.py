@@ -73,14 +73,16 @@ def runs(native, oracle_mod, problem):
     return out
 
 
-@pytest.mark.parametrize("K", [1, 3, 100])
-def test_checkpointed_records_give_identical_kernels(native, problem, runs, K):
-    """Checkpoints every K records + segment recompute = keeping every record, bit for bit."""
+@pytest.mark.parametrize("K,K2", [(1, 0), (3, 0), (100, 0), (5, 2), (12, 5), (4, 3)])
+def test_checkpointed_records_give_identical_kernels(native, problem, runs, K, K2):
+    """Checkpoints every K records + segment recompute (K2 = 0), or two levels (segments of
+    K records recomputed into checkpoints every K2 records, sub-segments recomputed from
+    those) = keeping every record, bit for bit."""
     from ses3d_gb300 import _lib
     from ses3d_gb300.solver import Simulation
     p = problem
     sim = Simulation.from_problem(p, adjoint_flag=1, grad_variant=1)
-    _lib.check(sim.lib.ses3d_gpu_set_checkpointing(sim.h, K), sim.h)
+    _lib.check(sim.lib.ses3d_gpu_set_checkpoint_levels(sim.h, K, K2), sim.h)
     sim.run()
     assert sim.record_count() == len(runs["gpu_records"])
     assert np.array_equal(sim.saving_vector(), runs["gpu_sv"])
@@ -92,6 +94,14 @@ def test_checkpointed_records_give_identical_kernels(native, problem, runs, K):
     for k in ("rho", "cp", "csh", "csv", "Q_mu"):
         assert np.array_equal(sim.kernel(k), runs["gpu_kernels"][k]), k
     sim.close()
+
+
+def test_checkpoint_levels_rejects_bad_lengths(native, problem):
+    from ses3d_gb300.solver import Simulation
+    with Simulation.from_problem(problem, adjoint_flag=1) as sim:
+        for K, K2 in ((4, 4), (0, 2), (-1, 0), (3, -2)):
+            assert sim.lib.ses3d_gpu_set_checkpoint_levels(sim.h, K, K2) == -1
+        assert sim.lib.ses3d_gpu_set_checkpoint_levels(sim.h, 4, 2) == 0
 
 
 def test_saving_vector(runs):

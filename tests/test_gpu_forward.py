@@ -366,10 +366,12 @@ def test_autotune_picks_a_candidate_and_keeps_results(native):
     """The block-shape autotuner steps the run forward on each candidate and leaves the
     fastest selected; the results equal an untuned run bit for bit."""
     from ses3d_gb300.solver import Simulation
-    p = synth.make_problem("tiny", nt=30, seed=8)
+    p = synth.make_problem("tiny", nt=40, seed=8)
     with Simulation.from_problem(p) as a:
         tuned = a.autotune(steps_each=2)
-        assert set(tuned) == {1, 2, 4} and a.it == 6 and all(v > 0 for v in tuned.values())
+        n_el = len(tuned["element"])
+        assert n_el >= 6 and len(tuned["node"]) == 3 and a.it == 3 * (n_el + 3)
+        assert all(v > 0 for v in tuned["element"].values())
         a.run()
         va = a.field("vz_global")
     with Simulation.from_problem(p) as b:
