@@ -268,26 +268,31 @@ def run_ours(args, rank, world, local):
             t.numpy()[:] = v
             pinned[k] = t.numpy()
         ev = p.events[0]
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        cfg_sim = Simulation.from_problem(p, nt=args.steps, model=False)
-        cfg_sim.set_lean(args.lean)
-        cfg_sim.set_block_elements(args.epb)
-        cfg_sim.set_kernel_shape(shape["element_shape"], shape["node_block"])
-        cfg_sim.set_model(pinned)
-        if args.graph:
-            cfg_sim.use_graph(True, args.graph)
-        cfg_sim.step(args.steps)
-        out = cfg_sim.seismograms(0)
-        t1 = time.perf_counter()
-        nr = cfg_sim.n_receivers(0)
-        cfg_sim.close()
-        t_e2e = max_over_ranks(t1 - t0, world)
+        # three independent runs (handle creation to seismograms each); the median is reported
+        # (host work and the host-to-device link are shared with other jobs on the machine)
+        secs = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            cfg_sim = Simulation.from_problem(p, nt=args.steps, model=False)
+            cfg_sim.set_lean(args.lean)
+            cfg_sim.set_block_elements(args.epb)
+            cfg_sim.set_kernel_shape(shape["element_shape"], shape["node_block"])
+            cfg_sim.set_model(pinned)
+            if args.graph:
+                cfg_sim.use_graph(True, args.graph)
+            cfg_sim.step(args.steps)
+            out = cfg_sim.seismograms(0)
+            t1 = time.perf_counter()
+            cfg_sim.close()
+            secs.append(max_over_ranks(t1 - t0, world))
+        t_e2e = sorted(secs)[1]
         h2d = sum(a.nbytes for a in pinned.values()) + 4 * args.steps + ev.receivers.loc.nbytes + 24
         d2h = sum(o.nbytes for o in out)
         e2e = {"value": world * N * args.steps / t_e2e, "unit": METRIC,
                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-               "seconds": t_e2e, "includes": "create + model upload + %d steps + seismogram download" % args.steps}
+               "seconds": t_e2e, "seconds_each_run": secs, "statistic": "median of 3 runs",
+               "includes": "create + model upload + %d steps + seismogram download" % args.steps}
         del pinned
 
     res = {

@@ -328,7 +328,11 @@ int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int n);
  * seismograms with respect to the model records is the gradient of the discrete forward
  * run itself (what finite differences of the forward run converge to).
  * Call ses3d_gpu_exact_adjoint on a flag-0 handle before stepping: the forward run keeps a
- * full-state checkpoint every steps_per_checkpoint iterations (lean stepping must be off).
+ * full-state checkpoint every steps_per_checkpoint iterations. Lean stepping, chosen before
+ * the forward run starts and kept for it, is exact for runs whose starting state has the
+ * mirror stresses equal to their partners outside the PML (a run from rest): the
+ * transposed step reads the velocities, memory variables, assembled forces and the
+ * displacement gradients inside the PML, which lean iterations keep as full-state ones do.
  * After nt iterations, give each event's d misfit / d seismogram with
  * ses3d_gpu_exact_set_seismogram_adjoint (gx, gy, gz: (nr, nt) each, receiver fastest, the
  * layout of ses3d_gpu_get_seismograms; NULL = zero) and call ses3d_gpu_exact_backward: it
@@ -337,12 +341,14 @@ int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int n);
  * the event-summed d misfit / d record for which = 0..6: rhoinv, mu, lambda, A, B, C, Q
  * (N doubles, reference layout; device = 1: out is device memory on the handle's device).
  * Memory per event: ceil(nt / K) checkpoints of (36 N + 3 G) floats, K iteration slots of
- * (36 N + 6 G) floats, the adjoint state and 6 N + G doubles of gradient. With
- * steps_per_subsegment = K2 (0 < K2 < K) a second level: each segment of K iterations is
- * recomputed once into checkpoints every K2 iterations and each sub-segment of K2
- * iterations from those (one more forward pass), so K2 slots and ceil(K / K2) - 1 more
- * checkpoints instead of K slots (for 64 x 64 x 32, nt = 4000: K = 250, K2 = 16 need
- * about 120 GB against 320 GB with one level).
+ * (15 N + 6 G) floats (9 N + 6 G without attenuation: the displacement gradients, the
+ * memory-variable sums, velocity and assembled forces of the iteration), the adjoint state
+ * and 6 N + G doubles of gradient. With steps_per_subsegment = K2 (0 < K2 < K) a second
+ * level: each segment of K iterations is recomputed once into checkpoints every K2
+ * iterations and each sub-segment of K2 iterations from those (one more forward pass), so
+ * K2 slots and ceil(K / K2) - 1 more checkpoints instead of K slots (for 64 x 64 x 32,
+ * nt = 4000: one level, K = 91, needs about 226 GB; two levels, K = 364, K2 = 28, about
+ * 100 GB).
  * ses3d_gpu_exact_set_field / get_field access the adjoint state (field ids as
  * ses3d_gpu_get_field, without MM_global): set before the backward run it is the adjoint of
  * the final state (zero by default); read after it, the adjoint of the initial state. */
@@ -364,7 +370,9 @@ int ses3d_gpu_exact_set_field(ses3d_gpu *h, int event, int field, const float *i
  * switched off. The displacement gradients outside the PML are not integrated, so once a
  * lean iteration has run, ses3d_gpu_get_field(SES3D_FIELD_DXUX..DZUY) returns
  * SES3D_E_STATE (for the rest of the run, or until that field is set) instead of values
- * the reference would not produce. begin_adjoint switches lean stepping off. */
+ * the reference would not produce. begin_adjoint switches lean stepping off. On a handle
+ * with the exact adjoint enabled the choice cannot change once stepping has started
+ * (SES3D_E_STATE). */
 int ses3d_gpu_set_lean(ses3d_gpu *h, int enable);
 
 /* Element-kernel block shape: elements per CTA (1, 2 or 4); 0 selects the default.

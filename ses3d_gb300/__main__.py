@@ -1,8 +1,11 @@
 """Command-line runner.
 
   python -m ses3d_gb300 run --workload c4 --events 1 --steps 10 [--epb 1] [--graph 0] [--lean 0]
+          [--adjoint | --exact K [--exact-k2 K2]]
       generates a seeded workload in memory and runs it on cuda:0, printing the
-      per-iteration time (used for profiling captures and quick checks);
+      per-iteration time (used for profiling captures and quick checks); --adjoint adds the
+      reference's adjoint run with kernel correlation, --exact the exact discrete adjoint
+      (checkpoints every K iterations, a second level every K2) driven by the seismograms;
   python -m ses3d_gb300 generate --workload c1 --out DIR [--nt 1000]
       writes the workload as a reference directory tree (INPUT/, MODELS/MODELS/);
   python -m ses3d_gb300 adjoint-sources --seismograms OFD --out ADJOINT/1 --kind cc
@@ -35,6 +38,9 @@ def main(argv=None):
     r.add_argument("--lean", type=int, default=0, help="1: lean plain-forward stepping")
     r.add_argument("--seed", type=int, default=1234)
     r.add_argument("--adjoint", action="store_true", help="forward with records, then adjoint with kernels")
+    r.add_argument("--exact", type=int, default=0, help="forward with exact-adjoint checkpoints every EXACT "
+                   "iterations, then the exact backward run")
+    r.add_argument("--exact-k2", type=int, default=0, help="second checkpoint level of --exact")
     g = sub.add_parser("generate")
     g.add_argument("--workload", default="c1")
     g.add_argument("--out", required=True)
@@ -74,9 +80,11 @@ def main(argv=None):
     from . import build
     build.build()
     from .solver import Simulation
-    p = synth.make_problem(a.workload, nt=a.steps + 2, seed=a.seed, n_events=a.events)
+    p = synth.make_problem(a.workload, nt=a.steps + (1 if a.exact else 2), seed=a.seed, n_events=a.events)
     sim = Simulation.from_problem(p, adjoint_flag=1 if a.adjoint else None)
     sim.set_block_elements(a.epb)
+    if a.exact:
+        sim.exact_adjoint(a.exact, a.exact_k2)
     if a.lean:
         sim.set_lean(True)
     if a.graph:
@@ -93,6 +101,13 @@ def main(argv=None):
         t2 = time.perf_counter()
         sim.step(a.steps + 1)
         out["adjoint_ms_per_step"] = (time.perf_counter() - t2) * 1e3 / (a.steps + 1)
+    if a.exact:
+        for ev in range(sim.n_events):
+            sim.set_seismogram_adjoint(ev, *sim.seismograms(ev))
+        t2 = time.perf_counter()
+        sim.exact_backward()
+        out["exact_backward_ms_per_step"] = (time.perf_counter() - t2) * 1e3 / (a.steps + 1)
+        out["launches"] = sim.launch_count
     sim.close()
     print(json.dumps(out))
     return 0

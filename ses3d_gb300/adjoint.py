@@ -184,6 +184,7 @@ class MisfitSetup:
             sim.set_source(slot, e.xxs, e.yys, e.zzs, e.source_type, e.mom, e.stf)
             sim.set_receivers(slot, e.recloc)
         sim.exact_adjoint(K, K2)
+        sim.set_lean(True)        # the run starts at rest: lean iterations are exact for it
         sim.use_graph(True, 10)
         sim.run()
         return sim
@@ -198,7 +199,9 @@ class MisfitSetup:
         E = (c.nx + 1) * (c.ny + 1) * (c.nz + 1)
         N, G = 125.0 * E, float((4 * c.nx + 5) * (4 * c.ny + 5) * (4 * c.nz + 5))
         nt = int(c.nt)
-        ckpt, slot = (36.0 * N + 3.0 * G) * 4, (36.0 * N + 6.0 * G) * 4
+        # an iteration slot keeps the 9 displacement gradients, the 6 memory-variable sums
+        # (attenuation only), the velocity and the assembled forces
+        ckpt, slot = (36.0 * N + 3.0 * G) * 4, ((15.0 if c.is_diss else 9.0) * N + 6.0 * G) * 4
         shared = 64.0 * N + 12.0 * G
         event = (36.0 * N + 3.0 * G + 3.0 * N) * 4 + (39.0 * N + 6.0 * G) * 4 + (6.0 * N + G) * 8 + ckpt
         if self.checkpoint_steps:

@@ -46,10 +46,11 @@ __global__ void __launch_bounds__(256) k_adj_node1(const Consts c, const Ptrs p,
   const float sF = dt * imm;
   a.aF[o] = sF * mx; a.aF[o + c.G] = sF * my; a.aF[o + 2 * c.G] = sF * mz;
   a.av[o] = damp * mx; a.av[o + c.G] = damp * my; a.av[o + 2 * c.G] = damp * mz;
-  const double dF = (double)mx * (double)a.fg[o] + (double)my * (double)a.fg[o + c.G] +
-                    (double)mz * (double)a.fg[o + 2 * c.G];
+  // the iteration's term in FP32, accumulated in FP64 (one conversion and one add: FP64
+  // issue is scarce on this part)
+  const float dF = mx * a.fg[o] + my * a.fg[o + c.G] + mz * a.fg[o + 2 * c.G];
   double *gi = a.gimm + (size_t)ev * c.G + g;
-  *gi += (double)dt * dF;
+  *gi += (double)(dt * dF);
 }
 
 // k_adj_node2: per (global node, event); thread 0 of the grid steps the adjoint counter back.
@@ -85,7 +86,8 @@ __global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs 
   const size_t g = (size_t)(i * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
   const size_t ov = (size_t)ev * 3 * c.G + g;
   const size_t os = ((size_t)ev * c.E + e) * ELEM_STATE + nn;
-  const float *FS = a.fstate + os;  // forward state before the iteration
+  constexpr int SF = slot_fields(DISS);
+  const float *FS = a.fstate + ((size_t)ev * c.E + e) * (SF * 125) + nn;  // packed forward state before the iteration
   float *AS = a.astate + os;        // adjoint state: lambda_t in, lambda_{t-1} out
   const float dt = c.dt;
 
@@ -123,11 +125,11 @@ __global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs 
               Pzx = px + py, Pyz = px + pz, Pzy = px + py;
   float es[6];  // PML-modified, symmetrised strain rates of the iteration
   {
-    const float dxux = FS[F_DXUX * 125] + dt * exx, dyuy = FS[F_DYUY * 125] + dt * eyy;
-    const float dzuz = FS[F_DZUZ * 125] + dt * ezz, dxuy = FS[F_DXUY * 125] + dt * exy;
-    const float dyux = FS[F_DYUX * 125] + dt * eyx, dxuz = FS[F_DXUZ * 125] + dt * exz;
-    const float dzux = FS[F_DZUX * 125] + dt * ezx, dyuz = FS[F_DYUZ * 125] + dt * eyz;
-    const float dzuy = FS[F_DZUY * 125] + dt * ezy;
+    const float dxux = FS[(F_DXUX - F_DXUX) * 125] + dt * exx, dyuy = FS[(F_DYUY - F_DXUX) * 125] + dt * eyy;
+    const float dzuz = FS[(F_DZUZ - F_DXUX) * 125] + dt * ezz, dxuy = FS[(F_DXUY - F_DXUX) * 125] + dt * exy;
+    const float dyux = FS[(F_DYUX - F_DXUX) * 125] + dt * eyx, dxuz = FS[(F_DXUZ - F_DXUX) * 125] + dt * exz;
+    const float dzux = FS[(F_DZUX - F_DXUX) * 125] + dt * ezx, dyuz = FS[(F_DYUZ - F_DXUX) * 125] + dt * eyz;
+    const float dzuy = FS[(F_DZUY - F_DXUX) * 125] + dt * ezy;
     es[0] = exx + Pxx * dxux;
     es[1] = eyy + Pyy * dyuy;
     es[2] = ezz + Pzz * dzuz;
@@ -139,7 +141,7 @@ __global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs 
   if (DISS) {
 #pragma unroll
     for (int cc = 0; cc < 6; ++cc)
-      Md[cc] = FS[(F_M + 3 * cc) * 125] + FS[(F_M + 3 * cc + 1) * 125] + FS[(F_M + 3 * cc + 2) * 125];
+      Md[cc] = FS[(9 + cc) * 125];
   }
   const float *MT = p.mat + (size_t)e * ELEM_MAT + nn;
   const float clam = __ldg(MT + M_CLAM * MAT_ROW), c2mut = __ldg(MT + M_C2MUT * MAT_ROW);
@@ -302,7 +304,7 @@ cudaError_t launch_adjoint_element(int diss, const Consts &c, const Ptrs &p, con
 // ---------------------------------------------------------------------------------------
 // Gradient with respect to the model records (rhoinv, mu, lambda, A, B, C, Q) from the
 // coefficient and 1/MM gradients, summed over events, in the reference layout (FP64).
-// The coefficients follow SOURCE/ses3d_init.f90:47-61 (k_derive): with tau = 1/Q and
+// The coefficients follow SOURCE/ses3d_init.f90:47-61 (k_derive_blocked): with tau = 1/Q and
 // sD = sum D_p, kappa - 2 mu_tau / 3 = lambda - (2/3) sD tau mu, 2 mu_tau = 2 (1 + sD tau) mu,
 // 2 mu tau; elastic runs: lambda, 2 mu, 0. The mass matrix MM = -sum_q W_q / rhoinv_q
 // (SOURCE/ses3d_init.f90:254-279, W_q = w w w Jac r^2 sin(theta)) gives

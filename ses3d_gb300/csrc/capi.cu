@@ -36,8 +36,8 @@ cudaError_t launch_transpose_d(const double *in, double *out, long long rows, lo
                                cudaStream_t st);
 cudaError_t launch_misfit_gradient(const double *K, const double *tables, int ex, int ey, int ez, double s,
                                    const void *div, void *out, bool f64, cudaStream_t st);
-cudaError_t launch_derive(const float *raw, float *mat, float *gm, long long N, int is_diss, float sum_D_p,
-                          cudaStream_t st);
+cudaError_t launch_derive_blocked(const float *const rec[7], float *mat, float *gm, long long E, int y0, int y1,
+                                  int is_diss, float sum_D_p, cudaStream_t st);
 cudaError_t launch_mass(const Consts &c, const float *rhoinv, const float *z, const float *sinx, const float *w,
                         float Jac, float *MM, float *iMM, cudaStream_t st);
 cudaError_t launch_vmax(const float *v, long long G3, int nev, unsigned int *out, cudaStream_t st);
@@ -47,7 +47,6 @@ cudaError_t prepare_element_kernels();
 cudaError_t launch_sync_mirrors(const Consts &c, float *state, cudaStream_t st);
 cudaError_t launch_wait_selftest(int *err, unsigned long long limit_ns, cudaStream_t st);
 cudaError_t launch_sum_events_d(const double *grad, int slot, int nev, long long N, double *out, cudaStream_t st);
-cudaError_t launch_pack_mat(const float *ref, float *out, long long E, cudaStream_t st);
 cudaError_t launch_state_field(float *state_ev, int field, float *ref, long long E, int to_ref, cudaStream_t st);
 cudaError_t launch_adjoint_node1(const Consts &c, const Ptrs &p, const AdjPtrs &a, cudaStream_t st);
 cudaError_t launch_adjoint_node2(const Consts &c, const AdjPtrs &a, cudaStream_t st);
@@ -93,6 +92,7 @@ struct ses3d_gpu {
   Geometry geo;
   int device = 0;
   cudaStream_t st = nullptr;
+  cudaStream_t st2 = nullptr;  // model set-up kernels beside the host-to-device copies
   std::string err;
   int it = 0;
   int mode_flag = 0;  // current adjoint_flag
@@ -344,27 +344,29 @@ int check_event(ses3d_gpu *h, int event) {
   return SES3D_OK;
 }
 
-int set_model_common(ses3d_gpu *h, float *d_raw) {
-  const long long N = h->geo.N;
-  float *d_tmp = nullptr;
-  CK(h, dalloc(&d_tmp, (size_t)(NMAT + NGMAT) * N));
+// Launches the model set-up for node tiles y0 .. y1 - 1 of the derivation (4 tiles cover
+// every node) and, with mass, the mass matrix; rec: the 7 model records on the device.
+static cudaError_t model_kernels(ses3d_gpu *h, const float *const rec[7], int y0, int y1, bool mass, cudaStream_t st) {
   float sum_D_p = h->cfg.D_p[0];
   sum_D_p = sum_D_p + h->cfg.D_p[1];
   sum_D_p = sum_D_p + h->cfg.D_p[2];
-  cudaError_t e = launch_derive(d_raw, d_tmp, d_tmp + (size_t)NMAT * N, N, h->cfg.is_diss, sum_D_p, h->st);
-  if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "derive"); }
-  e = launch_pack_mat(d_tmp, h->d_mat, h->geo.E, h->st);
-  if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "pack material"); }
-  for (int f = 0; f < NGMAT; ++f) {
-    e = launch_transpose(d_tmp + (size_t)(NMAT + f) * N, h->d_gmat + (size_t)f * N, NPE, h->geo.E, h->st);
-    if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "transpose gmat"); }
+  cudaError_t e = cudaSuccess;
+  if (mass) {
+    e = launch_mass(h->c, rec[0], h->d_tab + h->o_z, h->d_tab + h->o_sin, h->d_tab + h->o_w, h->geo.Jac, h->d_MM,
+                    h->d_MM + h->geo.G, st);
+    ++h->launches;
   }
-  e = launch_mass(h->c, d_raw, h->d_tab + h->o_z, h->d_tab + h->o_sin, h->d_tab + h->o_w, h->geo.Jac, h->d_MM,
-                  h->d_MM + h->geo.G, h->st);
-  if (e != cudaSuccess) { dfree(d_tmp); return cuda_fail(h, e, "mass"); }
-  h->launches += 3 + NGMAT;
-  e = cudaStreamSynchronize(h->st);
-  dfree(d_tmp);
+  if (e == cudaSuccess && y1 > y0) {
+    e = launch_derive_blocked(rec, h->d_mat, h->d_gmat, h->geo.E, y0, y1, h->cfg.is_diss, sum_D_p, st);
+    ++h->launches;
+  }
+  return e;
+}
+
+// Model set-up from 7 records already on the device (reference layout), on the handle's stream.
+int set_model_common(ses3d_gpu *h, const float *const rec[7]) {
+  cudaError_t e = model_kernels(h, rec, 0, 4, true, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
   if (e != cudaSuccess) return cuda_fail(h, e, "set_model");
   h->model_set = true;
   return SES3D_OK;
@@ -425,9 +427,13 @@ Wave primary_wave(ses3d_gpu *h) {
 }
 
 // one iteration of a wavefield: receivers, element, inject, node (+ record / kernel work)
-int launch_iteration(ses3d_gpu *h, const Wave &w, int mode, float *rec, bool timed = false, float *fg = nullptr) {
+// fg: also store the assembled forces there; slot: also pack the iteration's starting state
+// there for the exact adjoint (plain iterations only).
+int launch_iteration(ses3d_gpu *h, const Wave &w, int mode, float *rec, bool timed = false, float *fg = nullptr,
+                     float *slot = nullptr) {
   Ptrs p = make_ptrs(h);
   p.fg = fg;
+  p.slot = slot;
   p.state = w.state;
   p.v = w.v;
   p.d_it = w.d_it;
@@ -769,6 +775,7 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   cudaError_t e = cudaSuccess;
   auto chk = [&](cudaError_t x) { if (x != cudaSuccess && e == cudaSuccess) e = x; };
   chk(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+  chk(cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking));
   chk(dalloc(&h->d_ktab, 1));
   chk(dalloc(&h->d_tab, tab.size()));
   chk(dalloc(&h->d_MM, (size_t)2 * g.G));  // MM_global and its reciprocal
@@ -846,6 +853,7 @@ int ses3d_gpu_destroy(ses3d_gpu *h) {
     for (void *q : ex) dfree(q);
   }
   if (h->st) cudaStreamDestroy(h->st);
+  if (h->st2) cudaStreamDestroy(h->st2);
   delete h;
   return SES3D_OK;
 }
@@ -856,18 +864,44 @@ int ses3d_gpu_set_model(ses3d_gpu *h, const float *rhoinv, const float *mu, cons
   if (!h) return SES3D_E_CONFIG;
   if (!rhoinv || !mu || !lambda || !A || !B || !C) return fail(h, SES3D_E_CONFIG, "null model array");
   if (h->cfg.is_diss && !Q) return fail(h, SES3D_E_CONFIG, "Q is required when is_diss = 1");
-  const long long N = h->geo.N;
+  const long long N = h->geo.N, E = h->geo.E;
+  const int nrec = h->cfg.is_diss ? 7 : 6;
   float *d_raw = nullptr;
-  CK(h, dalloc(&d_raw, (size_t)7 * N));
+  CK(h, dalloc(&d_raw, (size_t)nrec * N));
   const float *src[7] = {rhoinv, mu, lambda, A, B, C, Q};
-  for (int k = 0; k < 7; ++k) {
-    if (!src[k]) continue;
-    cudaError_t e = cudaMemcpyAsync(d_raw + (size_t)k * N, src[k], N * sizeof(float), cudaMemcpyHostToDevice, h->st);
-    if (e != cudaSuccess) { dfree(d_raw); return cuda_fail(h, e, "set_model copy"); }
+  const float *rec[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  for (int k = 0; k < nrec; ++k) rec[k] = d_raw + (size_t)k * N;
+  // The copies run on the handle's stream: rhoinv first, then the other records in four node
+  // ranges (32 nodes of every element each, E floats per node). The set-up kernels run on
+  // the second stream behind them: the mass matrix once rhoinv has arrived, each node
+  // range's derivation once its records have, overlapping the copies still in flight.
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaError_t e = cudaSuccess;
+  for (int q = 0; q < 6 && e == cudaSuccess; ++q) e = cudaEventCreateWithFlags(&ev[q], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_raw, src[0], N * sizeof(float), cudaMemcpyHostToDevice, h->st);
+  if (e == cudaSuccess) e = cudaEventRecord(ev[0], h->st);
+  for (int t = 0; t < 4 && e == cudaSuccess; ++t) {
+    const long long n0 = 32 * t, n1 = t == 3 ? 125 : 32 * t + 32;
+    for (int k = 1; k < nrec && e == cudaSuccess; ++k)
+      e = cudaMemcpyAsync(d_raw + (size_t)k * N + n0 * E, src[k] + n0 * E, (size_t)(n1 - n0) * E * sizeof(float),
+                          cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1 + t], h->st);
   }
-  int rc = set_model_common(h, d_raw);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(h->st2, ev[0], 0);
+  if (e == cudaSuccess) e = model_kernels(h, rec, 0, 0, true, h->st2);
+  for (int t = 0; t < 4 && e == cudaSuccess; ++t) {
+    e = cudaStreamWaitEvent(h->st2, ev[1 + t], 0);
+    if (e == cudaSuccess) e = model_kernels(h, rec, t, t + 1, false, h->st2);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(ev[5], h->st2);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(h->st, ev[5], 0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  for (cudaEvent_t x : ev)
+    if (x) cudaEventDestroy(x);
   dfree(d_raw);
-  return rc;
+  if (e != cudaSuccess) return cuda_fail(h, e, "set_model");
+  h->model_set = true;
+  return SES3D_OK;
 }
 
 int ses3d_gpu_set_model_device(ses3d_gpu *h, const float *rhoinv, const float *mu, const float *lambda,
@@ -875,18 +909,8 @@ int ses3d_gpu_set_model_device(ses3d_gpu *h, const float *rhoinv, const float *m
   if (!h) return SES3D_E_CONFIG;
   if (!rhoinv || !mu || !lambda || !A || !B || !C) return fail(h, SES3D_E_CONFIG, "null model array");
   if (h->cfg.is_diss && !Q) return fail(h, SES3D_E_CONFIG, "Q is required when is_diss = 1");
-  const long long N = h->geo.N;
-  float *d_raw = nullptr;
-  CK(h, dalloc(&d_raw, (size_t)7 * N));
-  const float *src[7] = {rhoinv, mu, lambda, A, B, C, Q};
-  for (int k = 0; k < 7; ++k) {
-    if (!src[k]) continue;
-    cudaError_t e = cudaMemcpyAsync(d_raw + (size_t)k * N, src[k], N * sizeof(float), cudaMemcpyDeviceToDevice, h->st);
-    if (e != cudaSuccess) { dfree(d_raw); return cuda_fail(h, e, "set_model_device copy"); }
-  }
-  int rc = set_model_common(h, d_raw);
-  dfree(d_raw);
-  return rc;
+  const float *rec[7] = {rhoinv, mu, lambda, A, B, C, h->cfg.is_diss ? Q : nullptr};
+  return set_model_common(h, rec);
 }
 
 int ses3d_gpu_set_source(ses3d_gpu *h, int event, float xxs_deg, float yys_deg, float zzs, int source_type,
@@ -1510,7 +1534,7 @@ int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
   bytes += h->segbuf.size() * nev * NREC * N * sizeof(float);
   bytes += h->ckpt2.size() * ckpt_floats(h) * sizeof(float);
   bytes += h->ex_ckpts.size() * ckpt_floats(h) * sizeof(float);
-  bytes += h->ex_slots.size() * nev * ((size_t)NSTATE * N + 6 * G) * sizeof(float);
+  bytes += h->ex_slots.size() * nev * ((size_t)slot_fields(h->cfg.is_diss) * N + 6 * G) * sizeof(float);
   bytes += h->ex_ckpts2.size() * ckpt_floats(h) * sizeof(float);
   if (h->d_astate) bytes += nev * (((size_t)NSTATE * N + 6 * G + 3 * N) * sizeof(float) + ((size_t)NMAT * N + G) * sizeof(double));
   if (h->d_state2) bytes += nev * ((size_t)NSTATE * N + 3 * G) * sizeof(float);
@@ -1521,8 +1545,10 @@ int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
 int ses3d_gpu_set_lean(ses3d_gpu *h, int enable) {
   if (!h) return SES3D_E_CONFIG;
   if (enable && h->mode_flag != 0) return fail(h, SES3D_E_CONFIG, "lean stepping applies to plain forward runs only");
-  if (enable && h->ex_K > 0)
-    return fail(h, SES3D_E_CONFIG, "the exact adjoint replays full-state iterations; lean stepping is off for it");
+  // An exact-adjoint run replays its iterations from checkpoints in the same stepping as its
+  // forward run, so the choice is made before that run starts and kept.
+  if (h->ex_K > 0 && h->it != 0 && (enable != 0) != (h->c.lean != 0))
+    return fail(h, SES3D_E_STATE, "lean stepping of an exact-adjoint run is chosen before its forward run starts");
   if (!enable) {
     int rc = sync_mirrors(h);
     if (rc) return rc;
@@ -1584,7 +1610,6 @@ int ses3d_gpu_exact_adjoint(ses3d_gpu *h, int steps_per_checkpoint, int steps_pe
     return fail(h, SES3D_E_CONFIG, "steps_per_subsegment must be 0 or between 1 and steps_per_checkpoint - 1");
   if (h->it != 0 || h->external_stepped)
     return fail(h, SES3D_E_STATE, "enable the exact adjoint before the forward run starts");
-  if (h->c.lean) return fail(h, SES3D_E_CONFIG, "switch lean stepping off before enabling the exact adjoint");
   const size_t nev = h->cfg.n_events, N = h->geo.N, G = h->geo.G;
   if (!h->d_astate) {
     CK(h, dalloc(&h->d_astate, nev * NSTATE * N));
@@ -1687,6 +1712,7 @@ int ses3d_gpu_exact_backward(ses3d_gpu *h) {
   if (rc) return rc;
   const size_t nev = h->cfg.n_events, N = h->geo.N, G = h->geo.G;
   const size_t ns = nev * NSTATE * N, nv = nev * 3 * G;
+  const size_t nsl = nev * (size_t)slot_fields(h->cfg.is_diss) * N;  // packed forward state of an iteration slot
   CK(h, cudaMemsetAsync(h->d_egmat, 0, nev * NMAT * N * sizeof(double), h->st));
   CK(h, cudaMemsetAsync(h->d_egimm, 0, nev * G * sizeof(double), h->st));
   const int ait0 = nt - 1;
@@ -1694,7 +1720,7 @@ int ses3d_gpu_exact_backward(ses3d_gpu *h) {
   const int K2 = h->ex_K2 > 0 ? h->ex_K2 : K;  // iterations recomputed into slots at a time
   while ((int)h->ex_slots.size() < std::min(K2, nt)) {
     float *q = nullptr;
-    CK(h, dalloc(&q, ns + 2 * nv));
+    CK(h, dalloc(&q, nsl + 2 * nv));
     h->ex_slots.push_back(q);
   }
   const int nsub_max = (std::min(K, nt) + K2 - 1) / K2;
@@ -1737,15 +1763,14 @@ int ses3d_gpu_exact_backward(ses3d_gpu *h) {
         if (rc) return rc;
         for (int t = a0 + 1; t <= a1; ++t) {
           float *slot = h->ex_slots[t - a0 - 1];
-          CK(h, cudaMemcpyAsync(slot, h->d_state2, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
-          CK(h, cudaMemcpyAsync(slot + ns, h->d_v2, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
-          rc = launch_iteration(h, w, 0, nullptr, false, slot + ns + nv);
+          CK(h, cudaMemcpyAsync(slot + nsl, h->d_v2, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+          rc = launch_iteration(h, w, 0, nullptr, false, slot + nsl + nv, slot);
           if (rc) return rc;
         }
       }
       for (int t = a1; t > a0; --t) {  // backward iterations a1 .. a0 + 1
         const float *slot = h->ex_slots[t - a0 - 1];
-        a.fstate = slot; a.fv = slot + ns; a.fg = slot + ns + nv;
+        a.fstate = slot; a.fv = slot + nsl; a.fg = slot + nsl + nv;
         CK(h, launch_adjoint_node1(h->c, p, a, h->st));
         CK(h, launch_adjoint_element(h->cfg.is_diss, h->c, p, a, h->st));
         if (h->fseis.n)

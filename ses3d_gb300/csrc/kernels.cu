@@ -566,8 +566,10 @@ __device__ __forceinline__ void gather_v_async(const Consts &c, const Ptrs &p, l
 }
 
 // MINB: resident CTAs per SM requested from ptxas (register cap); REFILL: when the next
-// item's bulk copy is issued (0: the measured rule below, 1: the other point).
-template <bool DISS, int MODE, int MINB = SES3D_TMA_MINB, int REFILL = 0>
+// item's bulk copy is issued (0: the measured rule below, 1: the other point). PACK: also
+// write the fields of each item's starting state that the exact adjoint's transposed step
+// reads (displacement gradients, memory-variable sums) to p.slot.
+template <bool DISS, int MODE, int MINB = SES3D_TMA_MINB, int REFILL = 0, bool PACK = false>
 __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const Ptrs p) {
   extern __shared__ __align__(128) unsigned char smem[];
   ElemStage *stage = reinterpret_cast<ElemStage *>(smem);
@@ -639,6 +641,16 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
       clam = sm[M_CLAM * MAT_ROW]; c2mut = sm[M_C2MUT * MAT_ROW];
       if (DISS) c2mt = sm[M_C2MT * MAT_ROW];
       cA = sm[M_A * MAT_ROW]; cB2 = sm[M_B2 * MAT_ROW]; cC = sm[M_C * MAT_ROW];
+      if (PACK) {  // the gradients (zero outside the PML in lean items: they enter nothing there)
+        constexpr int SF = slot_fields(DISS);
+        float *D = p.slot + ((size_t)ev * c.E + e) * (SF * 125) + nn;
+#pragma unroll
+        for (int f = 0; f < 9; ++f) D[f * 125] = sv[F_DXUX + f];
+        if (DISS) {
+#pragma unroll
+          for (int cc = 0; cc < 6; ++cc) D[(9 + cc) * 125] = sv[F_M + 3 * cc] + sv[F_M + 3 * cc + 1] + sv[F_M + 3 * cc + 2];
+        }
+      }
     } else {
 #pragma unroll
       for (int f = 0; f < NS; ++f) sv[f] = 0.f;
@@ -674,8 +686,8 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
     float *S = p.state + ((size_t)ev * c.E + e) * ELEM_STATE + nn;
     const float *lt = (TMA_VBUF == 2 && TABLES) ? s_lt + LT_FLOATS * (t % 2) : nullptr;
     ElemCtx x{on, full, n, nn, in, jn, kn, i, j, k, ev, e, (size_t)c.N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC, lt};
-    if (LATE_REFILL) element_compute<DISS, (MODE == 3 ? 3 : 0)>(c, p, *tab, s_v, s_p, x, sv, issue_refill);
-    else element_compute<DISS, (MODE == 3 ? 3 : 0)>(c, p, *tab, s_v, s_p, x, sv);
+    if (LATE_REFILL) element_compute<DISS, MODE>(c, p, *tab, s_v, s_p, x, sv, issue_refill);
+    else element_compute<DISS, MODE>(c, p, *tab, s_v, s_p, x, sv);
   }
 }
 
@@ -853,40 +865,89 @@ __global__ void k_misfit_gradient(const double *__restrict__ K, const double *__
 }
 
 // ---------------------------------------------------------------------------------------
-// Model derivation (reference layout, elementwise; SOURCE/ses3d_input.f90:499,
-// SOURCE/ses3d_init.f90:47-61). Rounding follows the reference (no contraction).
-// raw = {rhoinv, mu, lambda, A, B, C, Q} (7 x N), out mat (NMAT x N), gm (NGMAT x N).
+// Model derivation (SOURCE/ses3d_input.f90:499, SOURCE/ses3d_init.f90:47-61; rounding as
+// the reference, no contraction) fused with the change of layout. In: the model records
+// rec[0..6] = rhoinv, mu, lambda, A, B, C, Q in the reference layout (element fastest:
+// index e + E n; Q may be null without attenuation). Out: the stress-rate coefficients
+// element-blocked, mat[e][NMAT][128] (nodes 125..127 zero), and the adjoint quantities
+// gm[f][e * 125 + n]. One 32 x 32 tile (elements e0.., nodes n0..) per 256-thread CTA:
+// reads coalesced along e, writes along n through shared memory. grid (ceil(E / 32),
+// node tiles) from node tile y0; block (32, 8).
 // ---------------------------------------------------------------------------------------
-__global__ void k_derive(const float *__restrict__ raw, float *__restrict__ mat, float *__restrict__ gm, long long N,
-                         int is_diss, float sum_D_p) {
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= N) return;
-  const float rhoinv = raw[q], mu = raw[N + q], lam = raw[2 * N + q];
-  const float A = raw[3 * N + q], B = raw[4 * N + q], C = raw[5 * N + q];
+struct ModelRecords {
+  const float *r[7];
+};
+
+__device__ __forceinline__ void derive_point(const ModelRecords &m, long long q, int is_diss, float sum_D_p,
+                                             float out[NMAT + NGMAT]) {
+  const float rhoinv = m.r[0][q], mu = m.r[1][q], lam = m.r[2][q];
+  const float A = m.r[3][q], B = m.r[4][q], C = m.r[5][q];
   const float kappa = __fadd_rn(lam, __fdiv_rn(__fmul_rn(2.f, mu), 3.f));
   float tau = 0.f, QQ = 0.f, mu_tau = 0.f;
   if (is_diss) {
-    QQ = raw[6 * N + q];
+    QQ = m.r[6][q];
     tau = __fdiv_rn(1.f, QQ);
     mu_tau = __fmul_rn(__fadd_rn(1.f, __fmul_rn(sum_D_p, tau)), mu);
-    mat[M_CLAM * N + q] = __fsub_rn(kappa, __fdiv_rn(__fmul_rn(2.f, mu_tau), 3.f));
-    mat[M_C2MUT * N + q] = __fmul_rn(2.f, mu_tau);
-    mat[M_C2MT * N + q] = __fmul_rn(__fmul_rn(2.f, mu), tau);
+    out[M_CLAM] = __fsub_rn(kappa, __fdiv_rn(__fmul_rn(2.f, mu_tau), 3.f));
+    out[M_C2MUT] = __fmul_rn(2.f, mu_tau);
+    out[M_C2MT] = __fmul_rn(__fmul_rn(2.f, mu), tau);
   } else {
-    mat[M_CLAM * N + q] = lam;
-    mat[M_C2MUT * N + q] = __fmul_rn(2.f, mu);
-    mat[M_C2MT * N + q] = 0.f;
+    out[M_CLAM] = lam;
+    out[M_C2MUT] = __fmul_rn(2.f, mu);
+    out[M_C2MT] = 0.f;
   }
-  mat[M_A * N + q] = A;
-  mat[M_B2 * N + q] = __fmul_rn(2.f, B);
-  mat[M_C * N + q] = C;
-  if (gm) {
-    gm[G_CS * N + q] = sqrtf(__fmul_rn(mu, rhoinv));
-    gm[G_CP * N + q] = sqrtf(__fmul_rn(__fadd_rn(lam, __fmul_rn(2.f, mu)), rhoinv));
-    gm[G_RHO * N + q] = rhoinv > 0.f ? __fdiv_rn(1.f, rhoinv) : 0.f;
-    gm[G_MU * N + q] = mu;
-    gm[G_KAPPA * N + q] = kappa;
-    gm[G_QQ * N + q] = QQ;
+  out[M_A] = A;
+  out[M_B2] = __fmul_rn(2.f, B);
+  out[M_C] = C;
+  out[NMAT + G_CS] = sqrtf(__fmul_rn(mu, rhoinv));
+  out[NMAT + G_CP] = sqrtf(__fmul_rn(__fadd_rn(lam, __fmul_rn(2.f, mu)), rhoinv));
+  out[NMAT + G_RHO] = rhoinv > 0.f ? __fdiv_rn(1.f, rhoinv) : 0.f;
+  out[NMAT + G_MU] = mu;
+  out[NMAT + G_KAPPA] = kappa;
+  out[NMAT + G_QQ] = QQ;
+}
+
+__global__ void __launch_bounds__(256) k_derive_blocked(const ModelRecords m, float *__restrict__ mat,
+                                                        float *__restrict__ gm, long long E, int y0, int is_diss,
+                                                        float sum_D_p) {
+  __shared__ float tile[NMAT][32][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const long long e0 = (long long)blockIdx.x * 32;
+  const int n0 = (y0 + (int)blockIdx.y) * 32;
+  const long long N = E * 125;
+  float v[4][NMAT + NGMAT];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {  // node n0 + ty + 8 a of element e0 + tx
+    const int n = n0 + ty + 8 * a;
+    const long long e = e0 + tx;
+    if (n < 125 && e < E) {
+      derive_point(m, (long long)n * E + e, is_diss, sum_D_p, v[a]);
+    } else {
+#pragma unroll
+      for (int f = 0; f < NMAT + NGMAT; ++f) v[a][f] = 0.f;
+    }
+  }
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {  // coefficients, then the adjoint quantities
+    if (half) __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int f = 0; f < NMAT; ++f) tile[f][ty + 8 * a][tx] = v[a][half * NMAT + f];
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {  // element e0 + ty + 8 a, node n0 + tx
+      const long long e = e0 + ty + 8 * a;
+      const int n = n0 + tx;
+      if (e >= E) continue;
+      if (half == 0 && n < MAT_ROW) {
+#pragma unroll
+        for (int f = 0; f < NMAT; ++f) mat[e * ELEM_MAT + f * MAT_ROW + n] = tile[f][tx][ty + 8 * a];
+      } else if (half == 1 && n < 125) {
+#pragma unroll
+        for (int f = 0; f < NGMAT; ++f) gm[f * N + e * 125 + n] = tile[f][tx][ty + 8 * a];
+      }
+    }
   }
 }
 
@@ -1036,14 +1097,14 @@ template <> struct TmaShape<2> { static constexpr int minb = 6, refill = 0; };
 template <> struct TmaShape<3> { static constexpr int minb = 5, refill = 1; };
 
 // Resident CTAs of one instantiation of k_element_tma on the current device (set by prepare_tma).
-template <bool DISS, int MODE, int S>
+template <bool DISS, int MODE, int S, bool PACK = false>
 static int &tma_grid_cap() {
   static int cap = 0;
   return cap;
 }
-template <bool DISS, int MODE, int S>
+template <bool DISS, int MODE, int S, bool PACK = false>
 static cudaError_t prepare_tma() {
-  auto kern = k_element_tma<DISS, MODE, TmaShape<S>::minb, TmaShape<S>::refill>;
+  auto kern = k_element_tma<DISS, MODE, TmaShape<S>::minb, TmaShape<S>::refill, PACK>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TMA_SMEM);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
@@ -1051,7 +1112,7 @@ static cudaError_t prepare_tma() {
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TPE, TMA_SMEM);
   if (e != cudaSuccess) return e;
-  tma_grid_cap<DISS, MODE, S>() = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  tma_grid_cap<DISS, MODE, S, PACK>() = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
   return cudaSuccess;
 }
 template <int S>
@@ -1066,19 +1127,27 @@ static cudaError_t prepare_tma_shape() {
 // when a handle is created, before any stream capture.
 cudaError_t prepare_element_kernels() {
   cudaError_t e;
+  if ((e = prepare_tma<false, 1, 0>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<false, 2, 0>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<true, 1, 0>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<true, 2, 0>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<false, 0, 0, true>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<false, 3, 0, true>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<true, 0, 0, true>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<true, 3, 0, true>()) != cudaSuccess) return e;
   if ((e = prepare_tma_shape<0>()) != cudaSuccess) return e;
   if ((e = prepare_tma_shape<1>()) != cudaSuccess) return e;
   if ((e = prepare_tma_shape<2>()) != cudaSuccess) return e;
   return prepare_tma_shape<3>();
 }
 
-template <bool DISS, int MODE, int S>
+template <bool DISS, int MODE, int S, bool PACK = false>
 static cudaError_t launch_tma(const Consts &c, const Ptrs &p, cudaStream_t st) {
-  const int grid_cap = tma_grid_cap<DISS, MODE, S>();
+  const int grid_cap = tma_grid_cap<DISS, MODE, S, PACK>();
   if (grid_cap <= 0) return cudaErrorInitializationError;
   const long long total = c.E * (long long)c.nev;
   const unsigned blocks = (unsigned)(total < grid_cap ? total : grid_cap);
-  k_element_tma<DISS, MODE, TmaShape<S>::minb, TmaShape<S>::refill><<<blocks, TPE, TMA_SMEM, st>>>(c, p);
+  k_element_tma<DISS, MODE, TmaShape<S>::minb, TmaShape<S>::refill, PACK><<<blocks, TPE, TMA_SMEM, st>>>(c, p);
   return cudaGetLastError();
 }
 
@@ -1095,9 +1164,20 @@ static cudaError_t launch_tma_shape(int shape, const Consts &c, const Ptrs &p, c
 int element_shape_count() { return kTmaShapes; }
 
 // shape: block shape of the persistent kernel (epb 1); epb 2, 4: register-staged kernel.
+// Record (1) and correlation (2) iterations run the persistent kernel in the default shape
+// 0 (they are one iteration in samp_ad; the searched shapes serve the plain iterations).
+// With p.slot set (plain or lean iterations), the persistent kernel in shape 0 also packs
+// each item's starting state into the slot, whatever epb and shape say.
 cudaError_t launch_element(int diss, int mode, int epb, int shape, const Consts &c, const Ptrs &p, cudaStream_t st) {
   if (mode == 0 && c.lean) mode = 3;
-  if (epb <= 1 && (mode == 0 || mode == 3)) {  // persistent TMA-pipelined kernel
+  if (p.slot) {
+    if (mode == 0) return diss ? launch_tma<true, 0, 0, true>(c, p, st) : launch_tma<false, 0, 0, true>(c, p, st);
+    if (mode == 3) return diss ? launch_tma<true, 3, 0, true>(c, p, st) : launch_tma<false, 3, 0, true>(c, p, st);
+    return cudaErrorInvalidValue;
+  }
+  if (epb <= 1) {  // persistent bulk-copy-pipelined kernel
+    if (mode == 1) return diss ? launch_tma<true, 1, 0>(c, p, st) : launch_tma<false, 1, 0>(c, p, st);
+    if (mode == 2) return diss ? launch_tma<true, 2, 0>(c, p, st) : launch_tma<false, 2, 0>(c, p, st);
     if (diss) return mode == 3 ? launch_tma_shape<true, 3>(shape, c, p, st) : launch_tma_shape<true, 0>(shape, c, p, st);
     return mode == 3 ? launch_tma_shape<false, 3>(shape, c, p, st) : launch_tma_shape<false, 0>(shape, c, p, st);
   }
@@ -1191,22 +1271,21 @@ cudaError_t launch_misfit_gradient(const double *K, const double *tables, int ex
   return cudaGetLastError();
 }
 
-cudaError_t launch_derive(const float *raw, float *mat, float *gm, long long N, int is_diss, float sum_D_p,
-                          cudaStream_t st) {
-  k_derive<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(raw, mat, gm, N, is_diss, sum_D_p);
+// Node tiles y0 .. y1 - 1 (32 nodes each, 4 tiles cover 0..127) of the fused model
+// derivation; rec: the 7 model records (reference layout), Q null without attenuation.
+cudaError_t launch_derive_blocked(const float *const rec[7], float *mat, float *gm, long long E, int y0, int y1,
+                                  int is_diss, float sum_D_p, cudaStream_t st) {
+  if (y0 < 0 || y1 > 4 || y0 >= y1) return cudaErrorInvalidValue;
+  ModelRecords m;
+  for (int k = 0; k < 7; ++k) m.r[k] = rec[k];
+  k_derive_blocked<<<dim3((unsigned)((E + 31) / 32), (unsigned)(y1 - y0)), dim3(32, 8), 0, st>>>(m, mat, gm, E, y0,
+                                                                                              is_diss, sum_D_p);
   return cudaGetLastError();
 }
 
 cudaError_t launch_mass(const Consts &c, const float *rhoinv, const float *z, const float *sinx, const float *w,
                         float Jac, float *MM, float *iMM, cudaStream_t st) {
   k_mass<<<(unsigned)((c.G + 255) / 256), 256, 0, st>>>(c, rhoinv, z, sinx, w, Jac, MM, iMM);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_pack_mat(const float *ref, float *out, long long E, cudaStream_t st) {
-  // material: [e][NMAT][128], nodes 125..127 zero
-  k_blocked_ref<<<dim3((unsigned)((E + 31) / 32), 4, NMAT), dim3(32, 8), 0, st>>>(
-      out, ELEM_MAT, 0, MAT_ROW, const_cast<float *>(ref), E, 0, 1);
   return cudaGetLastError();
 }
 

@@ -60,6 +60,12 @@ struct Consts {
   double s_jac;   // samp_ad dt / Jac in FP64: the weight of one kernel-correlation term
 };
 
+// Fields of the forward state the backward iteration reads, packed per element into an
+// iteration slot: the 9 displacement gradients, then (with attenuation) the 6 per-component
+// sums of the 3 memory variables, Mxx .. Myz.
+constexpr int SLOT_FIELDS_DISS = 15, SLOT_FIELDS_ELASTIC = 9;
+__host__ __device__ constexpr int slot_fields(bool diss) { return diss ? SLOT_FIELDS_DISS : SLOT_FIELDS_ELASTIC; }
+
 struct Ptrs {
   const KTab *ktab;
   const float *sin_x, *cot_x, *r_z;     // [i*5+n], [k*5+n]
@@ -85,13 +91,15 @@ struct Ptrs {
   float *rec;                           // record of this iteration: [nev][NREC][N]
   double *grad;                         // [nev][NGRAD][N]
   int grad_q;                           // accumulate the Q kernels too
+  float *slot;                          // [nev][E][slot_fields][125]: the iteration's starting state,
+                                        // packed for the exact adjoint, or null
 };
 
 // Exact discrete adjoint of one iteration (adjoint.cu): the forward state the iteration
 // started from and the forces it assembled, the adjoint state, scratch and the FP64
 // gradient accumulators.
 struct AdjPtrs {
-  const float *fstate;                  // [nev][E][NSTATE][125] forward state before the iteration
+  const float *fstate;                  // [nev][E][slot_fields][125] packed forward state before the iteration
   const float *fv;                      // [nev][3][G] forward velocity before the iteration
   const float *fg;                      // [nev][3][G] assembled forces of the iteration
   float *astate;                        // [nev][E][NSTATE][125] adjoint state (in: after, out: before)

@@ -224,3 +224,35 @@ def test_exact_misfit_gradient_matches_finite_differences(c3_misfit):
               % (nm, fd, fds[1], fds[0], ge, err, gc, abs(gc - fd) / abs(fd)))
         assert abs(fd) > 0
         assert err <= 1e-3, (nm, fd, ge)
+
+
+@pytest.mark.parametrize("K,K2", [(7, 0), (7, 3)])
+def test_lean_forward_gives_the_same_gradient(native, K, K2):
+    """A run from rest stepped lean (elements outside the PML keep neither displacement
+    gradients nor mirror stresses) gives the exact gradient and the adjoint of the initial
+    state of the full-state run bit for bit, with one and two checkpoint levels; the
+    choice cannot change once the forward run has started."""
+    from ses3d_gb300 import _lib
+    from ses3d_gb300.solver import Simulation
+    nt = 30
+    p = synth.make_problem("small", nt=nt, seed=64)
+    out = []
+    for lean in (False, True):
+        with Simulation.from_problem(p) as sim:
+            sim.exact_adjoint(K, K2)
+            sim.set_lean(lean)
+            sim.step(5)
+            with pytest.raises(_lib.Ses3dError) as err:
+                sim.set_lean(not lean)
+            assert err.value.code == -4
+            sim.set_lean(lean)                      # the same choice again is accepted
+            sim.run()
+            seis = sim.seismograms(0)
+            assert np.abs(seis[2]).max() > 0
+            sim.set_seismogram_adjoint(0, *seis)
+            sim.exact_backward()
+            out.append(([sim.exact_gradient(r) for r in RECORDS],
+                        [sim.exact_field(k) for k in ("vx_global", "vz_global", "sxx_pml", "Mxx")]))
+    for a, b in zip(out[0][0] + out[0][1], out[1][0] + out[1][1]):
+        assert np.abs(a).max() > 0
+        assert np.array_equal(a, b)

@@ -59,3 +59,47 @@ def test_autotune_keeps_a_timed_candidate(native):
         it = sim.it
         sim.run()                                   # the run continues with the chosen shape
         assert sim.it == 60 and it < 60
+
+
+def adjoint_run(p, epb, nt):
+    """Forward with records (adjoint_flag 1), then the adjoint with the kernel correlation,
+    with the element kernel chosen by epb (1: persistent bulk-copy kernel, 2: register-staged)."""
+    from ses3d_gb300.solver import Simulation
+    sim = Simulation.from_problem(p, adjoint_flag=1, grad_variant=1)
+    try:
+        sim.set_block_elements(epb)
+        sim.run()
+        records = [sim.record(r) for r in range(sim.record_count())]
+        seis = sim.seismograms(0)
+        loc = p.events[0].receivers.loc[:2].copy()
+        stf = np.zeros((2, 3, nt), np.float32)
+        for k in range(2):
+            for c in range(3):
+                stf[k, c] = seis[c][k][::-1]
+        stf *= np.float32(1e10) / np.abs(stf).max()
+        sim.set_adjoint_sources(0, loc, stf)
+        sim.begin_adjoint()
+        sim.run()
+        names = ("rho", "cp", "csh", "csv") + (("Q_mu", "alpha_mu", "Q_kappa") if p.setup.is_diss else ())
+        kernels = [sim.kernel(k) for k in names]
+        return records, kernels
+    finally:
+        sim.close()
+
+
+@pytest.mark.parametrize("is_diss", [1, 0])
+def test_record_and_correlation_kernels_bit_identical(native, is_diss):
+    """Record (forward store) and kernel-correlation iterations give the same records and
+    Frechet kernels on the persistent element kernel as on the register-staged one."""
+    nt = 40
+    p = synth.make_problem("small", nt=nt, seed=84, adjoint_flag=1, is_diss=is_diss)
+    p.setup.samp_ad = 4
+    rec1, ker1 = adjoint_run(p, 1, nt)
+    rec2, ker2 = adjoint_run(p, 2, nt)
+    assert len(rec1) == len(rec2) == 1 + nt // 4   # iteration 1 and every samp_ad-th
+    assert np.abs(rec1[-1]).max() > 0      # the first record (iteration 1) is still zero
+    for a, b in zip(rec1, rec2):
+        assert np.array_equal(a, b)
+    assert len(ker1) == len(ker2) == (7 if is_diss else 4)
+    for k, (a, b) in enumerate(zip(ker1, ker2)):
+        assert np.abs(a).max() > 0 and np.array_equal(a, b), k
