@@ -34,6 +34,9 @@ METRIC = "GLL point-steps/s"
 STATE_B, MAT_B, UNIQ_B = 288.0, 24.0, 28.0
 # k_element alone: state + material + v gather (12 B x ratio).
 ELEM_UNIQ_B = 12.0
+# An isotropic model (A = B = C = 0, the library reports it) needs three of the six
+# material floats: the element kernels read 12 B per point of material then.
+MAT_ISO_B = 12.0
 
 
 def load_peak():
@@ -203,6 +206,8 @@ def run_ours(args, rank, world, local):
     DU_B = 96.0  # 9 displacement gradients + 3 mirror stresses, read + written
     sim = Simulation.from_problem(p)
     sim.set_lean(args.lean)
+    iso = bool(sim.setup_int("isotropic")[0])
+    mat_b = MAT_ISO_B if iso else MAT_B
     tuned = None
     args.autotuned = not args.epb
     if args.epb:
@@ -252,11 +257,11 @@ def run_ours(args, rank, world, local):
     rc_ms, rc_n = prof.kernel_time("receivers")
     prof.close()
     el_avg = el_ms / max(el_n, 1)
-    elem_bytes = N * (STATE_B + MAT_B + ELEM_UNIQ_B * r_u - DU_B * interior_frac)
+    elem_bytes = N * (STATE_B + mat_b + ELEM_UNIQ_B * r_u - DU_B * interior_frac)
     peak, peak_kind = load_peak()
     achieved = elem_bytes / (el_avg / 1e3) / 1e9
     tr = load_traffic(args.workload)
-    step_bytes = N * (STATE_B + MAT_B + UNIQ_B * r_u - DU_B * interior_frac)
+    step_bytes = N * (STATE_B + mat_b + UNIQ_B * r_u - DU_B * interior_frac)
     step_gbs = step_bytes / (ms / args.steps / 1e3) / 1e9
 
     # end to end through the public API with host buffers (pinned)
@@ -304,7 +309,8 @@ def run_ours(args, rank, world, local):
                         "graph_steps": args.graph,
                         "lean": bool(args.lean), "non_pml_element_fraction": (E - n_pml_el) / E,
                         "step_algorithmic_bytes_per_point": step_bytes / N,
-                        "step_algorithmic_bytes_per_point_full_state": STATE_B + MAT_B + UNIQ_B * r_u,
+                        "step_algorithmic_bytes_per_point_full_state": STATE_B + mat_b + UNIQ_B * r_u,
+                        "isotropic_model": iso, "material_bytes_per_point": mat_b,
                         "step_achieved_gbs": step_gbs, "step_frac_of_peak": step_gbs / peak,
                         "finite": finite, "steps_completed": steps_done,
                         "kernel_ms": {"k_element": el_avg, "k_node": nd_ms / max(nd_n, 1),
@@ -320,7 +326,7 @@ def run_ours(args, rank, world, local):
     if e2e:
         res["e2e"] = e2e
     if args.lean:
-        res["full_state"] = run_full_state(args, p, world, peak, STATE_B + MAT_B + UNIQ_B * r_u)
+        res["full_state"] = run_full_state(args, p, world, peak, STATE_B + mat_b + UNIQ_B * r_u)
     if not args.no_batched:
         res["batched"] = run_batched(args, world)
         res["forward_c1"] = run_forward_small(args, world)

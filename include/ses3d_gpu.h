@@ -240,7 +240,8 @@ int ses3d_gpu_begin_adjoint(ses3d_gpu *h);
 
 /* Setup quantities for bit-exact checks of the index work of ses3d_init.
  * Integers: "nr", "rx", "ry", "rz", "isx", "isy", "isz", "is_source", "nr_adsrc", "is"
- * (3 x nr_adsrc); reals: "recloc_std" (3 x nr), "xxs_loc", "yys_loc", "zzs_loc",
+ * (3 x nr_adsrc), "isotropic" (1 when the model's A, B and C records are all zero: the
+ * element kernels then read three of the six material fields per point); reals: "recloc_std" (3 x nr), "xxs_loc", "yys_loc", "zzs_loc",
  * "x", "y", "z" (element-node coordinates), "dl", "knots", "w", "Jac", "dx", "dy", "dz",
  * "prof_x", "prof_y", "prof_z", "taper" (N, reference layout). Returns the count
  * written (out may be NULL to query the size) or a negative code. */

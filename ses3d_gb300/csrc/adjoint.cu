@@ -123,13 +123,20 @@ __global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs 
                taper);
   const float Pxx = pz + py, Pyy = px + pz, Pzz = px + py, Pxy = py + pz, Pyx = px + pz, Pxz = py + pz,
               Pzx = px + py, Pyz = px + pz, Pzy = px + py;
+  // Outside the PML the profiles are zero: the forward displacement gradients enter nothing
+  // there and are neither packed nor read, and adjoint ones that start at zero stay zero.
+  const bool pml = in_pml_element(c, i, j, k);
+  const bool skip_ad = !pml && a.zero_d;
+  float fd[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) fd[q] = pml ? FS[q * 125] : 0.f;
   float es[6];  // PML-modified, symmetrised strain rates of the iteration
   {
-    const float dxux = FS[(F_DXUX - F_DXUX) * 125] + dt * exx, dyuy = FS[(F_DYUY - F_DXUX) * 125] + dt * eyy;
-    const float dzuz = FS[(F_DZUZ - F_DXUX) * 125] + dt * ezz, dxuy = FS[(F_DXUY - F_DXUX) * 125] + dt * exy;
-    const float dyux = FS[(F_DYUX - F_DXUX) * 125] + dt * eyx, dxuz = FS[(F_DXUZ - F_DXUX) * 125] + dt * exz;
-    const float dzux = FS[(F_DZUX - F_DXUX) * 125] + dt * ezx, dyuz = FS[(F_DYUZ - F_DXUX) * 125] + dt * eyz;
-    const float dzuy = FS[(F_DZUY - F_DXUX) * 125] + dt * ezy;
+    const float dxux = fd[0] + dt * exx, dyuy = fd[1] + dt * eyy;
+    const float dzuz = fd[2] + dt * ezz, dxuy = fd[3] + dt * exy;
+    const float dyux = fd[4] + dt * eyx, dxuz = fd[5] + dt * exz;
+    const float dzux = fd[6] + dt * ezx, dyuz = fd[7] + dt * eyz;
+    const float dzuy = fd[8] + dt * ezy;
     es[0] = exx + Pxx * dxux;
     es[1] = eyy + Pyy * dyuy;
     es[2] = ezz + Pzz * dzuz;
@@ -146,7 +153,8 @@ __global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs 
   const float *MT = p.mat + (size_t)e * ELEM_MAT + nn;
   const float clam = __ldg(MT + M_CLAM * MAT_ROW), c2mut = __ldg(MT + M_C2MUT * MAT_ROW);
   const float c2mt = DISS ? __ldg(MT + M_C2MT * MAT_ROW) : 0.f;
-  const float cA = __ldg(MT + M_A * MAT_ROW), cB2 = __ldg(MT + M_B2 * MAT_ROW), cC = __ldg(MT + M_C * MAT_ROW);
+  const float cA = c.iso ? 0.f : __ldg(MT + M_A * MAT_ROW), cB2 = c.iso ? 0.f : __ldg(MT + M_B2 * MAT_ROW);
+  const float cC = c.iso ? 0.f : __ldg(MT + M_C * MAT_ROW);
 
   // ---- weak divergence, in reverse: lambda of the weighted stresses
   const float lF0 = act ? a.aF[ov] : 0.f, lF1 = act ? a.aF[ov + c.G] : 0.f, lF2 = act ? a.aF[ov + 2 * c.G] : 0.f;
@@ -245,8 +253,8 @@ __global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs 
     const float P[9] = {Pxx, Pyy, Pzz, Pxy, Pyx, Pxz, Pzx, Pyz, Pzy};
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
-      const float lD = AS[(F_DXUX + q) * 125] + P[q] * l2[q];  // d' = d + dt e;  e2 = e + P d'
-      if (act) AS[(F_DXUX + q) * 125] = lD;
+      const float lD = skip_ad ? 0.f : AS[(F_DXUX + q) * 125] + P[q] * l2[q];  // d' = d + dt e;  e2 = e + P d'
+      if (act && !skip_ad) AS[(F_DXUX + q) * 125] = lD;
       lE[q] = l2[q] + dt * lD;
     }
   }

@@ -6,6 +6,13 @@
 
 namespace ses3d {
 
+// Whether element (i, j, k) lies in the PML: pml elements on both x and y sides and at the
+// bottom (the top is a free surface; SOURCE/ses3d_init.f90:586). Outside, every profile is
+// zero and the taper one.
+__device__ __forceinline__ bool in_pml_element(const Consts &c, int i, int j, int k) {
+  return i < c.pml || i >= c.ex - c.pml || j < c.pml || j >= c.ey - c.pml || k >= c.ez - c.pml;
+}
+
 // Column gy of a global-node index t = gx + GX gy, by the multiply-shift division the
 // constants hold (exact for 32-bit t, GX >= 2).
 __device__ __forceinline__ int node_row(const Consts &c, unsigned t) {

@@ -37,7 +37,7 @@ cudaError_t launch_transpose_d(const double *in, double *out, long long rows, lo
 cudaError_t launch_misfit_gradient(const double *K, const double *tables, int ex, int ey, int ez, double s,
                                    const void *div, void *out, bool f64, cudaStream_t st);
 cudaError_t launch_derive_blocked(const float *const rec[7], float *mat, float *gm, long long E, int y0, int y1,
-                                  int is_diss, float sum_D_p, cudaStream_t st);
+                                  int is_diss, float sum_D_p, int *aniso, cudaStream_t st);
 cudaError_t launch_mass(const Consts &c, const float *rhoinv, const float *z, const float *sinx, const float *w,
                         float Jac, float *MM, float *iMM, cudaStream_t st);
 cudaError_t launch_vmax(const float *v, long long G3, int nev, unsigned int *out, cudaStream_t st);
@@ -107,6 +107,8 @@ struct ses3d_gpu {
   float *d_tab = nullptr;  // sin_x | cot_x | r_z | pxr | pyr | pzr | pxg | pyg | pzg | z | w
   float *d_MM = nullptr, *d_mat = nullptr, *d_gmat = nullptr;
   float *d_state = nullptr, *d_v = nullptr, *d_f = nullptr;
+  bool state_zero = false;  // d_state holds zeros only (since zero_wavefield, before any step or field write)
+  int *d_aniso = nullptr;   // set by the model derivation when A, B or C is non-zero
   int *d_it = nullptr;
   int *d_err = nullptr;  // device error word (bounded waits)
   bool mirrors_stale = false;  // lean iterations left the mirror stresses outside the PML behind
@@ -160,6 +162,7 @@ struct ses3d_gpu {
   std::vector<std::vector<float>> seis_adj;  // per event: d misfit / d seismogram, [3][nt][nr]
   ForceSet fseis;                            // the receivers' adjoint sources as point forces
   bool ex_done = false;
+  bool ex_zero_d = true;  // the adjoint displacement gradients were not set (zero from the start)
   float *d_state2 = nullptr, *d_v2 = nullptr;  // wavefield of the recomputing forward run
   int *d_it2 = nullptr;
   std::vector<int> saving_vector;  // [nt+1]
@@ -357,16 +360,33 @@ static cudaError_t model_kernels(ses3d_gpu *h, const float *const rec[7], int y0
     ++h->launches;
   }
   if (e == cudaSuccess && y1 > y0) {
-    e = launch_derive_blocked(rec, h->d_mat, h->d_gmat, h->geo.E, y0, y1, h->cfg.is_diss, sum_D_p, st);
+    e = launch_derive_blocked(rec, h->d_mat, h->d_gmat, h->geo.E, y0, y1, h->cfg.is_diss, sum_D_p, h->d_aniso, st);
     ++h->launches;
   }
   return e;
 }
 
+// After the model kernels completed: isotropic models (A, B, C all zero) let the element
+// kernels read three of the six material fields. Kernel parameters captured in a CUDA
+// graph hold the old setting, so a change drops the graph.
+static cudaError_t note_isotropy(ses3d_gpu *h) {
+  int aniso = 1;
+  cudaError_t e = cudaMemcpy(&aniso, h->d_aniso, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return e;
+  const int iso = aniso ? 0 : 1;
+  if (iso != h->c.iso) {
+    h->c.iso = iso;
+    destroy_graph(h);
+  }
+  return cudaSuccess;
+}
+
 // Model set-up from 7 records already on the device (reference layout), on the handle's stream.
 int set_model_common(ses3d_gpu *h, const float *const rec[7]) {
-  cudaError_t e = model_kernels(h, rec, 0, 4, true, h->st);
+  cudaError_t e = cudaMemsetAsync(h->d_aniso, 0, sizeof(int), h->st);
+  if (e == cudaSuccess) e = model_kernels(h, rec, 0, 4, true, h->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  if (e == cudaSuccess) e = note_isotropy(h);
   if (e != cudaSuccess) return cuda_fail(h, e, "set_model");
   h->model_set = true;
   return SES3D_OK;
@@ -382,6 +402,7 @@ int zero_wavefield(ses3d_gpu *h) {
   h->mirrors_stale = false;
   h->du_stale = 0;
   h->it = 0;
+  h->state_zero = true;
   return SES3D_OK;
 }
 
@@ -434,6 +455,7 @@ int launch_iteration(ses3d_gpu *h, const Wave &w, int mode, float *rec, bool tim
   Ptrs p = make_ptrs(h);
   p.fg = fg;
   p.slot = slot;
+  h->state_zero = false;
   p.state = w.state;
   p.v = w.v;
   p.d_it = w.d_it;
@@ -781,6 +803,7 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   chk(dalloc(&h->d_MM, (size_t)2 * g.G));  // MM_global and its reciprocal
   chk(dalloc(&h->d_mat, (size_t)ELEM_MAT * g.E));
   chk(dalloc(&h->d_err, 1));
+  chk(dalloc(&h->d_aniso, 1));
   chk(dalloc(&h->d_gmat, (size_t)NGMAT * g.N));
   chk(dalloc(&h->d_state, nev * NSTATE * g.N));
   chk(dalloc(&h->d_v, nev * 3 * g.G));
@@ -798,6 +821,13 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
     cudaGetLastError();  // clear the failed allocation's last error
     ses3d_gpu_destroy(h);
     return fail(nullptr, e == cudaErrorMemoryAllocation ? SES3D_E_OOM : SES3D_E_CUDA, m);
+  }
+  // zero the wavefield first: the memsets run on the handle's stream while the tables below
+  // are uploaded and the kernels prepared
+  if (int rc0 = zero_wavefield(h)) {
+    std::string m = h->err;
+    ses3d_gpu_destroy(h);
+    return fail(nullptr, rc0, m);
   }
   chk(cudaMemcpy(h->d_ktab, &kt, sizeof(KTab), cudaMemcpyHostToDevice));
   chk(cudaMemcpy(h->d_tab, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice));
@@ -821,9 +851,12 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   h->saving_vector.assign(cfg->nt + 2, 0);
   for (int it = 1; it <= cfg->nt; ++it)  // stored iterations of a flag-1 run (ses3d_main.f90:144)
     if (cfg->samp_ad > 0 && (it % cfg->samp_ad == 0 || it == 1 || it == cfg->nt)) h->store_steps.push_back(it);
-  int rc = zero_wavefield(h);
-  if (rc) { std::string m = h->err; ses3d_gpu_destroy(h); return fail(nullptr, rc, m); }
-  cudaStreamSynchronize(h->st);
+  e = cudaStreamSynchronize(h->st);
+  if (e != cudaSuccess) {
+    std::string m = std::string("initialisation: ") + cudaGetErrorString(e);
+    ses3d_gpu_destroy(h);
+    return fail(nullptr, SES3D_E_CUDA, m);
+  }
   *out = h;
   return SES3D_OK;
 }
@@ -836,7 +869,8 @@ int ses3d_gpu_destroy(ses3d_gpu *h) {
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   void *ptrs[] = {h->d_ktab, h->d_tab, h->d_MM, h->d_mat, h->d_gmat, h->d_state, h->d_v, h->d_f, h->d_it,
                   h->d_src_elem, h->d_src_delta, h->d_src_mom, h->d_stf, h->d_src_none, h->d_rec_elem,
-                  h->d_rec_ev, h->d_rec_w, h->d_seis, h->d_grad, h->d_scratch_u, h->d_state2, h->d_v2, h->d_it2, h->d_err};
+                  h->d_rec_ev, h->d_rec_w, h->d_seis, h->d_grad, h->d_scratch_u, h->d_state2, h->d_v2, h->d_it2, h->d_err,
+                  h->d_aniso};
   for (void *p : ptrs) dfree(p);
   free_forces(h->fset[0]);
   free_forces(h->fset[1]);
@@ -866,8 +900,11 @@ int ses3d_gpu_set_model(ses3d_gpu *h, const float *rhoinv, const float *mu, cons
   if (h->cfg.is_diss && !Q) return fail(h, SES3D_E_CONFIG, "Q is required when is_diss = 1");
   const long long N = h->geo.N, E = h->geo.E;
   const int nrec = h->cfg.is_diss ? 7 : 6;
-  float *d_raw = nullptr;
-  CK(h, dalloc(&d_raw, (size_t)nrec * N));
+  // Staging for the records: the element state while it holds zeros only (a handle that has
+  // not stepped; at least 36 N floats), zeroed again afterwards; else a buffer of its own.
+  const bool in_state = h->state_zero;
+  float *d_raw = in_state ? h->d_state : nullptr;
+  if (!in_state) CK(h, dalloc(&d_raw, (size_t)nrec * N));
   const float *src[7] = {rhoinv, mu, lambda, A, B, C, Q};
   const float *rec[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   for (int k = 0; k < nrec; ++k) rec[k] = d_raw + (size_t)k * N;
@@ -887,6 +924,7 @@ int ses3d_gpu_set_model(ses3d_gpu *h, const float *rhoinv, const float *mu, cons
                           cudaMemcpyHostToDevice, h->st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[1 + t], h->st);
   }
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->d_aniso, 0, sizeof(int), h->st2);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(h->st2, ev[0], 0);
   if (e == cudaSuccess) e = model_kernels(h, rec, 0, 0, true, h->st2);
   for (int t = 0; t < 4 && e == cudaSuccess; ++t) {
@@ -895,10 +933,20 @@ int ses3d_gpu_set_model(ses3d_gpu *h, const float *rhoinv, const float *mu, cons
   }
   if (e == cudaSuccess) e = cudaEventRecord(ev[5], h->st2);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(h->st, ev[5], 0);
+  if (e == cudaSuccess && in_state) e = cudaMemsetAsync(d_raw, 0, (size_t)nrec * N * sizeof(float), h->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  if (e == cudaSuccess) e = note_isotropy(h);
   for (cudaEvent_t x : ev)
     if (x) cudaEventDestroy(x);
-  dfree(d_raw);
+  if (in_state) {
+    if (e != cudaSuccess) {  // the staged records may remain in the state: zero it again
+      cudaStreamSynchronize(h->st);
+      cudaStreamSynchronize(h->st2);
+      cudaMemset(d_raw, 0, (size_t)nrec * N * sizeof(float));
+    }
+  } else {
+    dfree(d_raw);
+  }
   if (e != cudaSuccess) return cuda_fail(h, e, "set_model");
   h->model_set = true;
   return SES3D_OK;
@@ -1130,10 +1178,12 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
   if (field < 0 || field >= SES3D_FIELD_COUNT) return fail(h, SES3D_E_CONFIG, "unknown field");
   if (h->external_stepped && field != SES3D_FIELD_MM_GLOBAL)
     return fail(h, SES3D_E_STATE, "the wavefield of this handle lives in caller-owned buffers (ses3d_gpu_step_external)");
-  if (hout && field >= SES3D_FIELD_DXUX && field <= SES3D_FIELD_DZUY && ((h->du_stale >> (field - SES3D_FIELD_DXUX)) & 1u))
+  if (hout && !adjoint && field >= SES3D_FIELD_DXUX && field <= SES3D_FIELD_DZUY &&
+      ((h->du_stale >> (field - SES3D_FIELD_DXUX)) & 1u))
     return fail(h, SES3D_E_STATE,
                 "lean iterations did not integrate this displacement gradient outside the PML (set_lean)");
   const long long N = h->geo.N, G = h->geo.G;
+  if (hin && !adjoint) h->state_zero = false;
   float *vbase = (adjoint ? h->d_av : h->d_v) + (size_t)event * 3 * G;
   float *sbase = (adjoint ? h->d_astate : h->d_state) + (size_t)event * NSTATE * N;
   if (field >= SES3D_FIELD_VX_GLOBAL && field <= SES3D_FIELD_VZ_GLOBAL) {
@@ -1384,6 +1434,7 @@ long ses3d_gpu_get_setup_int(ses3d_gpu *h, int event, const char *name, int *out
   auto one = [&](int v) -> long { if (out) out[0] = v; return 1; };
   auto vec = [&](const std::vector<int> &v) -> long { if (out) std::copy(v.begin(), v.end(), out); return (long)v.size(); };
   if (nm == "nr") return one((int)E.recs.size());
+  if (nm == "isotropic") return one(h->c.iso);
   if (nm == "rx" || nm == "ry" || nm == "rz") {
     std::vector<int> v;
     for (const Receiver &r : E.recs) v.push_back(nm == "rx" ? r.rx : nm == "ry" ? r.ry : r.rz);
@@ -1625,6 +1676,7 @@ int ses3d_gpu_exact_adjoint(ses3d_gpu *h, int steps_per_checkpoint, int steps_pe
   CK(h, cudaStreamSynchronize(h->st));
   h->ex_K = steps_per_checkpoint;
   h->ex_K2 = steps_per_subsegment;
+  h->ex_zero_d = true;
   h->seis_adj.assign(nev, std::vector<float>());
   h->ex_done = false;
   destroy_graph(h);
@@ -1734,6 +1786,7 @@ int ses3d_gpu_exact_backward(ses3d_gpu *h) {
   std::memset(&a, 0, sizeof(a));
   a.astate = h->d_astate; a.av = h->d_av; a.aF = h->d_aF; a.af = h->d_af;
   a.gmat = h->d_egmat; a.gimm = h->d_egimm; a.d_ait = h->d_ait;
+  a.zero_d = h->ex_zero_d ? 1 : 0;
   rc = ensure_wave2(h);  // the recomputing wavefield must exist before its pointers are taken
   if (rc) return rc;
   const Wave w{h->d_state2, h->d_v2, h->d_it2, false, false};
@@ -1826,6 +1879,7 @@ int ses3d_gpu_exact_set_field(ses3d_gpu *h, int event, int field, const float *i
   if (!in) return fail(h, SES3D_E_CONFIG, "null input");
   if (!h->d_astate) return fail(h, SES3D_E_STATE, "enable the exact adjoint first (ses3d_gpu_exact_adjoint)");
   if (field == SES3D_FIELD_MM_GLOBAL) return fail(h, SES3D_E_CONFIG, "MM_global is not part of the adjoint state");
+  if (field >= SES3D_FIELD_DXUX && field <= SES3D_FIELD_DZUY) h->ex_zero_d = false;
   return field_io(h, event, field, nullptr, in, true);
 }
 

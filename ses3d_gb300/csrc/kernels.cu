@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
     for (int f = F_DZUY + 1; f < NS; ++f) sv[f] = S[f * 125];
     clam = __ldg(MT + M_CLAM * MAT_ROW); c2mut = __ldg(MT + M_C2MUT * MAT_ROW);
     if (DISS) c2mt = __ldg(MT + M_C2MT * MAT_ROW);
-    cA = __ldg(MT + M_A * MAT_ROW); cB2 = __ldg(MT + M_B2 * MAT_ROW); cC = __ldg(MT + M_C * MAT_ROW);
+    if (!c.iso) { cA = __ldg(MT + M_A * MAT_ROW); cB2 = __ldg(MT + M_B2 * MAT_ROW); cC = __ldg(MT + M_C * MAT_ROW); }
   } else {
 #pragma unroll
     for (int f = 0; f < NS; ++f) sv[f] = 0.f;
@@ -489,9 +489,6 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
                : "memory");
 }
 
-__device__ __forceinline__ bool in_pml_element(const Consts &c, int i, int j, int k) {
-  return i < c.pml || i >= c.ex - c.pml || j < c.pml || j >= c.ey - c.pml || k >= c.ez - c.pml;
-}
 
 // Copies of one item into a stage. Byte ranges (element block of 18,000 B, fields of 500 B):
 // all 36 fields; elastic: fields 0-17 (9,008 B, the last 8 B inside field 18); lean outside
@@ -507,7 +504,7 @@ __device__ __forceinline__ void issue_item(const Consts &c, const Ptrs &p, long 
   const char *src = reinterpret_cast<const char *>(p.state + ((size_t)ev * c.E + e) * ELEM_STATE);
   const char *msrc = reinterpret_cast<const char *>(p.mat + (size_t)e * ELEM_MAT);
   char *dst = reinterpret_cast<char *>(st->state);
-  constexpr unsigned MB = ELEM_MAT * sizeof(float);
+  const unsigned MB = (c.iso ? 3 * MAT_ROW : ELEM_MAT) * (unsigned)sizeof(float);
   if (!DISS && MODE == 3 && !in_pml_element(c, i, j, k)) {
     mbar_arrive_expect_tx(bar, 3008u + MB);
     bulk_g2s(dst, src, 3008u, bar);
@@ -640,12 +637,15 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
       for (int f = F_DZUY + 1; f < NS; ++f) sv[f] = ss[f * 125];
       clam = sm[M_CLAM * MAT_ROW]; c2mut = sm[M_C2MUT * MAT_ROW];
       if (DISS) c2mt = sm[M_C2MT * MAT_ROW];
-      cA = sm[M_A * MAT_ROW]; cB2 = sm[M_B2 * MAT_ROW]; cC = sm[M_C * MAT_ROW];
-      if (PACK) {  // the gradients (zero outside the PML in lean items: they enter nothing there)
+      if (!c.iso) { cA = sm[M_A * MAT_ROW]; cB2 = sm[M_B2 * MAT_ROW]; cC = sm[M_C * MAT_ROW]; }
+      if (PACK) {  // displacement gradients in PML elements only: outside, the transposed step
+                   // multiplies them by zero profiles and does not read them
         constexpr int SF = slot_fields(DISS);
         float *D = p.slot + ((size_t)ev * c.E + e) * (SF * 125) + nn;
+        if (in_pml_element(c, i, j, k)) {
 #pragma unroll
-        for (int f = 0; f < 9; ++f) D[f * 125] = sv[F_DXUX + f];
+          for (int f = 0; f < 9; ++f) D[f * 125] = sv[F_DXUX + f];
+        }
         if (DISS) {
 #pragma unroll
           for (int cc = 0; cc < 6; ++cc) D[(9 + cc) * 125] = sv[F_M + 3 * cc] + sv[F_M + 3 * cc + 1] + sv[F_M + 3 * cc + 2];
@@ -909,24 +909,27 @@ __device__ __forceinline__ void derive_point(const ModelRecords &m, long long q,
 
 __global__ void __launch_bounds__(256) k_derive_blocked(const ModelRecords m, float *__restrict__ mat,
                                                         float *__restrict__ gm, long long E, int y0, int is_diss,
-                                                        float sum_D_p) {
+                                                        float sum_D_p, int *__restrict__ aniso) {
   __shared__ float tile[NMAT][32][33];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const long long e0 = (long long)blockIdx.x * 32;
   const int n0 = (y0 + (int)blockIdx.y) * 32;
   const long long N = E * 125;
   float v[4][NMAT + NGMAT];
+  bool nz = false;  // a non-zero (or NaN) A, B or C
 #pragma unroll
   for (int a = 0; a < 4; ++a) {  // node n0 + ty + 8 a of element e0 + tx
     const int n = n0 + ty + 8 * a;
     const long long e = e0 + tx;
     if (n < 125 && e < E) {
       derive_point(m, (long long)n * E + e, is_diss, sum_D_p, v[a]);
+      nz = nz || !(v[a][M_A] == 0.f) || !(v[a][M_B2] == 0.f) || !(v[a][M_C] == 0.f);
     } else {
 #pragma unroll
       for (int f = 0; f < NMAT + NGMAT; ++f) v[a][f] = 0.f;
     }
   }
+  if (__any_sync(0xffffffffu, nz) && tx == 0) atomicOr(aniso, 1);  // a warp is one row ty
 #pragma unroll
   for (int half = 0; half < 2; ++half) {  // coefficients, then the adjoint quantities
     if (half) __syncthreads();
@@ -1274,12 +1277,12 @@ cudaError_t launch_misfit_gradient(const double *K, const double *tables, int ex
 // Node tiles y0 .. y1 - 1 (32 nodes each, 4 tiles cover 0..127) of the fused model
 // derivation; rec: the 7 model records (reference layout), Q null without attenuation.
 cudaError_t launch_derive_blocked(const float *const rec[7], float *mat, float *gm, long long E, int y0, int y1,
-                                  int is_diss, float sum_D_p, cudaStream_t st) {
+                                  int is_diss, float sum_D_p, int *aniso, cudaStream_t st) {
   if (y0 < 0 || y1 > 4 || y0 >= y1) return cudaErrorInvalidValue;
   ModelRecords m;
   for (int k = 0; k < 7; ++k) m.r[k] = rec[k];
-  k_derive_blocked<<<dim3((unsigned)((E + 31) / 32), (unsigned)(y1 - y0)), dim3(32, 8), 0, st>>>(m, mat, gm, E, y0,
-                                                                                              is_diss, sum_D_p);
+  k_derive_blocked<<<dim3((unsigned)((E + 31) / 32), (unsigned)(y1 - y0)), dim3(32, 8), 0, st>>>(
+      m, mat, gm, E, y0, is_diss, sum_D_p, aniso);
   return cudaGetLastError();
 }
 

@@ -53,6 +53,8 @@ struct Consts {
   float q_alpha_w[3];  // dP/dalpha_k tau_k / D_k of the alpha kernels (ses3d_grad_Q.f90:126)
   int pml;        // PML width in elements
   int lean;       // plain forward: displacement gradients kept only in PML elements
+  int iso;        // the model's A, B and C records are zero: the element kernels read the
+                  // first three material fields only (the others multiply zeros)
   // t / GX for 32-bit t as (m + ((t - m) >> 1)) >> shift with m = umulhi(t, gx_magic)
   // (division by an invariant integer, Granlund & Montgomery 1994); GX >= 2
   unsigned gx_magic;
@@ -109,6 +111,8 @@ struct AdjPtrs {
   double *gmat;                         // [nev][E][NMAT][125] d misfit / d stress-rate coefficient
   double *gimm;                         // [nev][G] d misfit / d (1 / MM)
   int *d_ait;                           // iteration counter of the backward run (iteration - 1)
+  int zero_d;                           // the adjoint displacement gradients outside the PML are
+                                        // zero (a backward run started with them zero keeps them so)
 };
 
 }  // namespace ses3d

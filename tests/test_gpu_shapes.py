@@ -103,3 +103,30 @@ def test_record_and_correlation_kernels_bit_identical(native, is_diss):
     assert len(ker1) == len(ker2) == (7 if is_diss else 4)
     for k, (a, b) in enumerate(zip(ker1, ker2)):
         assert np.abs(a).max() > 0 and np.array_equal(a, b), k
+
+
+def test_isotropy_follows_the_model_and_drops_the_graph(native):
+    """The model's A, B, C decide whether the element kernels read three or six material
+    fields: an isotropic model reports 1, a model with non-zero A, B, C set later in the run
+    reports 0, and a CUDA graph captured before the change is not replayed with the old
+    setting: graph and eager stepping agree bit for bit across the switch."""
+    from ses3d_gb300.solver import Simulation
+    p = synth.make_problem("small", nt=24, seed=85)
+    m = dict(p.model)
+    rng = np.random.default_rng(5)
+    mu = np.asarray(p.model["mu"], np.float64)
+    for k, s in (("A", 0.02), ("B", 0.03), ("C", -0.02)):
+        m[k] = (s * mu * rng.uniform(0.5, 1.0, mu.size)).astype(np.float32)
+    out = []
+    for graph in (True, False):
+        with Simulation.from_problem(p) as sim:
+            assert sim.setup_int("isotropic")[0] == 1
+            if graph:
+                sim.use_graph(True, 4)
+            sim.step(12)
+            sim.set_model(m)
+            assert sim.setup_int("isotropic")[0] == 0
+            sim.step(12)
+            out.append([sim.field("vx_global"), sim.field("sxz_pml"), np.concatenate(sim.seismograms(0))])
+    for a, b in zip(*out):
+        assert np.abs(a).max() > 0 and np.array_equal(a, b)
