@@ -69,8 +69,9 @@ __global__ void __launch_bounds__(256) k_adj_node2(const Consts c, const AdjPtrs
 }
 
 // k_adj_element: one element per 128-thread CTA (thread = GLL node); grid (ex, ey, ez * nev).
+// Every global load of the element is issued first, before the first barrier.
 template <bool DISS>
-__global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs p, const AdjPtrs a) {
+__global__ void __launch_bounds__(TPE, 4) k_adj_element(const Consts c, const Ptrs p, const AdjPtrs a) {
   __shared__ KTab tab;
   __shared__ float s_a[9][TPE];
   for (int q = threadIdx.x; q < KTAB_FLOATS; q += TPE)
@@ -91,9 +92,47 @@ __global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs 
   float *AS = a.astate + os;        // adjoint state: lambda_t in, lambda_{t-1} out
   const float dt = c.dt;
 
+  // Outside the PML the profiles are zero: the forward displacement gradients enter nothing
+  // there and are neither packed nor read, and adjoint ones that start at zero stay zero.
+  const bool pml = in_pml_element(c, i, j, k);
+  const bool skip_ad = !pml && a.zero_d;
+
+  // ---- loads: forward velocity and the adjoint of the assembled forces at the element's
+  // nodes, the adjoint state, the packed forward state, the material and the 1-D tables
+  float vx = 0.f, vy = 0.f, vz = 0.f, lF0 = 0.f, lF1 = 0.f, lF2 = 0.f;
+  if (act) {
+    vx = a.fv[ov]; vy = a.fv[ov + c.G]; vz = a.fv[ov + 2 * c.G];
+    lF0 = a.aF[ov]; lF1 = a.aF[ov + c.G]; lF2 = a.aF[ov + 2 * c.G];
+  }
+  float as_s[9], as_d[9], as_m[DISS ? 18 : 1];
+#pragma unroll
+  for (int f = 0; f < 9; ++f) as_s[f] = AS[f * 125];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) as_d[q] = skip_ad ? 0.f : AS[(F_DXUX + q) * 125];
+  if (DISS) {
+#pragma unroll
+    for (int q = 0; q < 18; ++q) as_m[q] = AS[(F_M + q) * 125];
+  }
+  float fd[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) fd[q] = pml ? FS[q * 125] : 0.f;
+  float Md[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // forward memory-variable sums per component
+  if (DISS) {
+#pragma unroll
+    for (int cc = 0; cc < 6; ++cc) Md[cc] = FS[(9 + cc) * 125];
+  }
+  const float *MT = p.mat + (size_t)e * ELEM_MAT + nn;
+  const float clam = __ldg(MT + M_CLAM * MAT_ROW), c2mut = __ldg(MT + M_C2MUT * MAT_ROW);
+  const float c2mt = DISS ? __ldg(MT + M_C2MT * MAT_ROW) : 0.f;
+  const float cA = c.iso ? 0.f : __ldg(MT + M_A * MAT_ROW), cB2 = c.iso ? 0.f : __ldg(MT + M_B2 * MAT_ROW);
+  const float cC = c.iso ? 0.f : __ldg(MT + M_C * MAT_ROW);
+  const float r = __ldg(p.r_z + k * 5 + kn), st = __ldg(p.sin_x + i * 5 + in);
+  const float ir = __ldg(p.inv_r + k * 5 + kn);
+  const float irs = ir * __ldg(p.inv_sin + i * 5 + in);
+  const float ct = __ldg(p.cot_x + i * 5 + in);
+  const float pxr = __ldg(p.pxr + i * 5 + in), pyr = __ldg(p.pyr + j * 5 + jn), pzr = __ldg(p.pzr + k * 5 + kn);
+
   // ---- forward quantities of the iteration (as k_element computes them)
-  float vx = 0.f, vy = 0.f, vz = 0.f;
-  if (act) { vx = a.fv[ov]; vy = a.fv[ov + c.G]; vz = a.fv[ov + 2 * c.G]; }
   s_a[0][n] = vx; s_a[1][n] = vy; s_a[2][n] = vz;
   __syncthreads();
   float exx = 0.f, exy = 0.f, exz = 0.f, eyx = 0.f, eyy = 0.f, eyz = 0.f, ezx = 0.f, ezy = 0.f, ezz = 0.f;
@@ -105,10 +144,6 @@ __global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs 
     eyx = fmaf(s_a[0][iy], dyq, eyx); eyy = fmaf(s_a[1][iy], dyq, eyy); eyz = fmaf(s_a[2][iy], dyq, eyz);
     ezx = fmaf(s_a[0][iz], dzq, ezx); ezy = fmaf(s_a[1][iz], dzq, ezy); ezz = fmaf(s_a[2][iz], dzq, ezz);
   }
-  const float r = __ldg(p.r_z + k * 5 + kn), st = __ldg(p.sin_x + i * 5 + in);
-  const float ir = __ldg(p.inv_r + k * 5 + kn);
-  const float irs = ir * __ldg(p.inv_sin + i * 5 + in);
-  const float ct = __ldg(p.cot_x + i * 5 + in);
   ezz = -ezz;
   eyy = eyy * irs + (vz + vx * ct) * ir;
   exx = (vz + exx) * ir;
@@ -119,17 +154,9 @@ __global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs 
   exy = exy * ir;
   eyx = -vy * ct * ir + eyx * irs;
   float px, py, pz, prof, taper;
-  pml_profiles(__ldg(p.pxr + i * 5 + in), __ldg(p.pyr + j * 5 + jn), __ldg(p.pzr + k * 5 + kn), px, py, pz, prof,
-               taper);
+  pml_profiles(pxr, pyr, pzr, px, py, pz, prof, taper);
   const float Pxx = pz + py, Pyy = px + pz, Pzz = px + py, Pxy = py + pz, Pyx = px + pz, Pxz = py + pz,
               Pzx = px + py, Pyz = px + pz, Pzy = px + py;
-  // Outside the PML the profiles are zero: the forward displacement gradients enter nothing
-  // there and are neither packed nor read, and adjoint ones that start at zero stay zero.
-  const bool pml = in_pml_element(c, i, j, k);
-  const bool skip_ad = !pml && a.zero_d;
-  float fd[9];
-#pragma unroll
-  for (int q = 0; q < 9; ++q) fd[q] = pml ? FS[q * 125] : 0.f;
   float es[6];  // PML-modified, symmetrised strain rates of the iteration
   {
     const float dxux = fd[0] + dt * exx, dyuy = fd[1] + dt * eyy;
@@ -144,20 +171,8 @@ __global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs 
     es[4] = ((exz + Pxz * dxuz) + (ezx + Pzx * dzux)) * 0.5f;
     es[5] = ((eyz + Pyz * dyuz) + (ezy + Pzy * dzuy)) * 0.5f;
   }
-  float Md[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // forward memory-variable sums per component
-  if (DISS) {
-#pragma unroll
-    for (int cc = 0; cc < 6; ++cc)
-      Md[cc] = FS[(9 + cc) * 125];
-  }
-  const float *MT = p.mat + (size_t)e * ELEM_MAT + nn;
-  const float clam = __ldg(MT + M_CLAM * MAT_ROW), c2mut = __ldg(MT + M_C2MUT * MAT_ROW);
-  const float c2mt = DISS ? __ldg(MT + M_C2MT * MAT_ROW) : 0.f;
-  const float cA = c.iso ? 0.f : __ldg(MT + M_A * MAT_ROW), cB2 = c.iso ? 0.f : __ldg(MT + M_B2 * MAT_ROW);
-  const float cC = c.iso ? 0.f : __ldg(MT + M_C * MAT_ROW);
 
   // ---- weak divergence, in reverse: lambda of the weighted stresses
-  const float lF0 = act ? a.aF[ov] : 0.f, lF1 = act ? a.aF[ov + c.G] : 0.f, lF2 = act ? a.aF[ov + 2 * c.G] : 0.f;
   const float cx = tab.CX[jn][kn] * r, cy = tab.CY[in][kn] * r, cz = tab.CZ[in][jn] * st;
   __syncthreads();  // s_a (forward velocity) fully read
   const bool on = act;
@@ -180,15 +195,15 @@ __global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs 
   const float wx = tab.w[in] * st, wy = tab.w[jn], wz = tab.w[kn] * r * r;
   // lambda of the marched PML stresses s' (before the taper): divergence + stored (tapered) state.
   // State order: sxx syy szz sxy sxz syz syx szx szy; divergence order: xx xy xz | yx yy yz | zx zy zz.
-  const float lxx = wx * lsp[0] + taper * AS[F_SXX * 125];
-  const float lxy = wx * lsp[1] + taper * AS[F_SXY * 125];
-  const float lxz = wx * lsp[2] + taper * AS[F_SXZ * 125];
-  const float lyx = wy * lsp[3] + taper * AS[F_SYX * 125];
-  const float lyy = wy * lsp[4] + taper * AS[F_SYY * 125];
-  const float lyz = wy * lsp[5] + taper * AS[F_SYZ * 125];
-  const float lzx = wz * lsp[6] + taper * AS[F_SZX * 125];
-  const float lzy = wz * lsp[7] + taper * AS[F_SZY * 125];
-  const float lzz = wz * lsp[8] + taper * AS[F_SZZ * 125];
+  const float lxx = wx * lsp[0] + taper * as_s[F_SXX];
+  const float lxy = wx * lsp[1] + taper * as_s[F_SXY];
+  const float lxz = wx * lsp[2] + taper * as_s[F_SXZ];
+  const float lyx = wy * lsp[3] + taper * as_s[F_SYX];
+  const float lyy = wy * lsp[4] + taper * as_s[F_SYY];
+  const float lyz = wy * lsp[5] + taper * as_s[F_SYZ];
+  const float lzx = wz * lsp[6] + taper * as_s[F_SZX];
+  const float lzy = wz * lsp[7] + taper * as_s[F_SZY];
+  const float lzz = wz * lsp[8] + taper * as_s[F_SZZ];
   // PML stress march s' = s + dt (sigma - p s)
   if (act) {
     AS[F_SXX * 125] = lxx * (1.f - dt * px);
@@ -234,7 +249,7 @@ __global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs 
     for (int cc = 0; cc < 6; ++cc)
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
-        const float lM = AS[(F_M + 3 * cc + m) * 125];
+        const float lM = as_m[3 * cc + m];
         les[cc] -= c.L_k[m] * lM;
         if (act) AS[(F_M + 3 * cc + m) * 125] = (1.f - c.a_k[m]) * lM + lMd[cc];
       }
@@ -253,7 +268,7 @@ __global__ void __launch_bounds__(TPE) k_adj_element(const Consts c, const Ptrs 
     const float P[9] = {Pxx, Pyy, Pzz, Pxy, Pyx, Pxz, Pzx, Pyz, Pzy};
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
-      const float lD = skip_ad ? 0.f : AS[(F_DXUX + q) * 125] + P[q] * l2[q];  // d' = d + dt e;  e2 = e + P d'
+      const float lD = skip_ad ? 0.f : as_d[q] + P[q] * l2[q];  // d' = d + dt e;  e2 = e + P d'
       if (act && !skip_ad) AS[(F_DXUX + q) * 125] = lD;
       lE[q] = l2[q] + dt * lD;
     }
