@@ -342,7 +342,7 @@ int ses3d_gpu_step_external(ses3d_gpu *h, float *state, float *v, int n);
  * the event-summed d misfit / d record for which = 0..6: rhoinv, mu, lambda, A, B, C, Q
  * (N doubles, reference layout; device = 1: out is device memory on the handle's device).
  * Memory per event: ceil(nt / K) checkpoints of (36 N + 3 G) floats, K iteration slots of
- * (15 N + 6 G) floats (9 N + 6 G without attenuation: the displacement gradients, the
+ * (1876 E + 6 G) floats (1128 E + 6 G without attenuation: the displacement gradients, the
  * memory-variable sums, velocity and assembled forces of the iteration), the adjoint state
  * and 6 N + G doubles of gradient. With steps_per_subsegment = K2 (0 < K2 < K) a second
  * level: each segment of K iterations is recomputed once into checkpoints every K2

@@ -200,8 +200,9 @@ class MisfitSetup:
         N, G = 125.0 * E, float((4 * c.nx + 5) * (4 * c.ny + 5) * (4 * c.nz + 5))
         nt = int(c.nt)
         # an iteration slot keeps the 9 displacement gradients, the 6 memory-variable sums
-        # (attenuation only), the velocity and the assembled forces
-        ckpt, slot = (36.0 * N + 3.0 * G) * 4, ((15.0 if c.is_diss else 9.0) * N + 6.0 * G) * 4
+        # (attenuation only; element blocks of 1,876 or 1,128 floats), the velocity and the
+        # assembled forces
+        ckpt, slot = (36.0 * N + 3.0 * G) * 4, ((1876.0 if c.is_diss else 1128.0) * E + 6.0 * G) * 4
         shared = 64.0 * N + 12.0 * G
         event = (36.0 * N + 3.0 * G + 3.0 * N) * 4 + (39.0 * N + 6.0 * G) * 4 + (6.0 * N + G) * 8 + ckpt
         if self.checkpoint_steps:

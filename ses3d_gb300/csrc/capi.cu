@@ -44,6 +44,7 @@ cudaError_t launch_vmax(const float *v, long long G3, int nev, unsigned int *out
 cudaError_t launch_grad_q_norm(const Consts &c, const float *gm, double *grad, cudaStream_t st);
 cudaError_t launch_gather_ref(const Consts &c, const float *v, float *out, cudaStream_t st);
 cudaError_t prepare_element_kernels();
+cudaError_t prepare_adjoint_kernels();
 cudaError_t launch_sync_mirrors(const Consts &c, float *state, cudaStream_t st);
 cudaError_t launch_wait_selftest(int *err, unsigned long long limit_ns, cudaStream_t st);
 cudaError_t launch_sum_events_d(const double *grad, int slot, int nev, long long N, double *out, cudaStream_t st);
@@ -840,6 +841,7 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   chk(cudaMemset(h->d_MM, 0, (size_t)2 * g.G * sizeof(float)));
   chk(cudaMemset(h->d_err, 0, sizeof(int)));
   if (e == cudaSuccess) e = prepare_element_kernels();
+  if (e == cudaSuccess) e = prepare_adjoint_kernels();
   if (h->d_grad) chk(cudaMemset(h->d_grad, 0, nev * NGRAD * g.N * sizeof(double)));
   if (e != cudaSuccess) {
     std::string m = std::string("initialisation: ") + cudaGetErrorString(e);
@@ -1585,7 +1587,7 @@ int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
   bytes += h->segbuf.size() * nev * NREC * N * sizeof(float);
   bytes += h->ckpt2.size() * ckpt_floats(h) * sizeof(float);
   bytes += h->ex_ckpts.size() * ckpt_floats(h) * sizeof(float);
-  bytes += h->ex_slots.size() * nev * ((size_t)slot_fields(h->cfg.is_diss) * N + 6 * G) * sizeof(float);
+  bytes += h->ex_slots.size() * nev * ((size_t)slot_stride(h->cfg.is_diss) * h->geo.E + 6 * G) * sizeof(float);
   bytes += h->ex_ckpts2.size() * ckpt_floats(h) * sizeof(float);
   if (h->d_astate) bytes += nev * (((size_t)NSTATE * N + 6 * G + 3 * N) * sizeof(float) + ((size_t)NMAT * N + G) * sizeof(double));
   if (h->d_state2) bytes += nev * ((size_t)NSTATE * N + 3 * G) * sizeof(float);
@@ -1764,7 +1766,7 @@ int ses3d_gpu_exact_backward(ses3d_gpu *h) {
   if (rc) return rc;
   const size_t nev = h->cfg.n_events, N = h->geo.N, G = h->geo.G;
   const size_t ns = nev * NSTATE * N, nv = nev * 3 * G;
-  const size_t nsl = nev * (size_t)slot_fields(h->cfg.is_diss) * N;  // packed forward state of an iteration slot
+  const size_t nsl = nev * (size_t)slot_stride(h->cfg.is_diss) * h->geo.E;  // packed forward state of an iteration slot
   CK(h, cudaMemsetAsync(h->d_egmat, 0, nev * NMAT * N * sizeof(double), h->st));
   CK(h, cudaMemsetAsync(h->d_egimm, 0, nev * G * sizeof(double), h->st));
   const int ait0 = nt - 1;

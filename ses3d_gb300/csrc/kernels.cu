@@ -15,6 +15,7 @@
 // contributions in the reference loop order, without atomics, so runs are bit-reproducible.
 #include "kernels.cuh"
 #include "assembly.cuh"
+#include "pipeline.cuh"
 
 // Minimum resident CTAs per SM requested from ptxas for k_element (register cap).
 #ifndef SES3D_ELEM_MINB
@@ -441,55 +442,6 @@ constexpr size_t TMA_LT_OFF =
 constexpr size_t TMA_BAR_OFF = TMA_LT_OFF + TMA_VBUF * LT_FLOATS * sizeof(float);
 constexpr size_t TMA_SMEM = TMA_BAR_OFF + TMA_STAGES * sizeof(unsigned long long);
 
-__device__ __forceinline__ unsigned smem_addr(const void *ptr) { return (unsigned)__cvta_generic_to_shared(ptr); }
-
-__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.u32 %0, 1, 0, P;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Waits for phase `parity` of bar; gives up after limit_ns (2 s), recording the failure in *err.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity, int *err,
-                                                  unsigned long long limit_ns = 2000000000ull) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const unsigned long long t0 = global_ns();
-  while (!mbar_try_wait(bar, parity)) {
-    if (global_ns() - t0 > limit_ns) {
-      atomicExch(err, 2);
-      return false;
-    }
-  }
-  return true;
-}
-
-// 1-D bulk copy global -> shared, completing on bar (addresses 16-B aligned, bytes % 16 == 0).
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_addr(dst)),
-               "l"(src), "r"(bytes), "r"(smem_addr(bar))
-               : "memory");
-}
-
-
 // Copies of one item into a stage. Byte ranges (element block of 18,000 B, fields of 500 B):
 // all 36 fields; elastic: fields 0-17 (9,008 B, the last 8 B inside field 18); lean outside
 // the PML: fields 0-5 (3,008 B) and, with attenuation, 18-35 (from byte 8,992, 9,008 B),
@@ -522,14 +474,9 @@ __device__ __forceinline__ void issue_item(const Consts &c, const Ptrs &p, long 
   bulk_g2s(st->mat, msrc, MB, bar);
 }
 
-// Element-local velocity of one item gathered from the assembled field straight into
-// shared memory with 4-byte cp.async (ses3d_evolution.f90:27-51); one commit group.
-__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-}
-
-// The element-local velocity and, with TABLES, the item's 1-D table entries and source
-// element into lt (threads 0..15), in one commit group. (The table copies pay off in
+// The element-local velocity of one item, gathered from the assembled field straight into
+// shared memory with 4-byte cp.async (ses3d_evolution.f90:27-51), and, with TABLES, the
+// item's 1-D table entries and source element into lt (threads 0..15), in one commit group. (The table copies pay off in
 // lean iterations; with the full state they cost more than the loads they replace.)
 template <bool TABLES>
 __device__ __forceinline__ void gather_v_async(const Consts &c, const Ptrs &p, long long item, float (*dst)[TPE],
@@ -640,8 +587,7 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
       if (!c.iso) { cA = sm[M_A * MAT_ROW]; cB2 = sm[M_B2 * MAT_ROW]; cC = sm[M_C * MAT_ROW]; }
       if (PACK) {  // displacement gradients in PML elements only: outside, the transposed step
                    // multiplies them by zero profiles and does not read them
-        constexpr int SF = slot_fields(DISS);
-        float *D = p.slot + ((size_t)ev * c.E + e) * (SF * 125) + nn;
+        float *D = p.slot + ((size_t)ev * c.E + e) * slot_stride(DISS) + nn;
         if (in_pml_element(c, i, j, k)) {
 #pragma unroll
           for (int f = 0; f < 9; ++f) D[f * 125] = sv[F_DXUX + f];

@@ -67,6 +67,9 @@ struct Consts {
 // sums of the 3 memory variables, Mxx .. Myz.
 constexpr int SLOT_FIELDS_DISS = 15, SLOT_FIELDS_ELASTIC = 9;
 __host__ __device__ constexpr int slot_fields(bool diss) { return diss ? SLOT_FIELDS_DISS : SLOT_FIELDS_ELASTIC; }
+// Floats of one element's slot block: its fields rounded up to a multiple of 4 floats, so
+// that every block starts 16-byte aligned (1,876 and 1,128).
+__host__ __device__ constexpr int slot_stride(bool diss) { return (slot_fields(diss) * 125 + 3) & ~3; }
 
 struct Ptrs {
   const KTab *ktab;
@@ -93,7 +96,7 @@ struct Ptrs {
   float *rec;                           // record of this iteration: [nev][NREC][N]
   double *grad;                         // [nev][NGRAD][N]
   int grad_q;                           // accumulate the Q kernels too
-  float *slot;                          // [nev][E][slot_fields][125]: the iteration's starting state,
+  float *slot;                          // [nev][E][slot_stride]: the iteration's starting state,
                                         // packed for the exact adjoint, or null
 };
 
@@ -101,7 +104,7 @@ struct Ptrs {
 // started from and the forces it assembled, the adjoint state, scratch and the FP64
 // gradient accumulators.
 struct AdjPtrs {
-  const float *fstate;                  // [nev][E][slot_fields][125] packed forward state before the iteration
+  const float *fstate;                  // [nev][E][slot_stride] packed forward state before the iteration
   const float *fv;                      // [nev][3][G] forward velocity before the iteration
   const float *fg;                      // [nev][3][G] assembled forces of the iteration
   float *astate;                        // [nev][E][NSTATE][125] adjoint state (in: after, out: before)

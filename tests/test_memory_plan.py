@@ -55,11 +55,13 @@ def test_config5_gradient_fits_150_gb():
 
 def exact_bytes(elements, nt, K, K2, is_diss):
     """Checkpoint and slot bytes of one event of the exact adjoint, restated from the
-    library's allocation: checkpoints of 36 N + 3 G floats; slots of 15 N + 6 G floats with
-    attenuation (9 N + 6 G without)."""
+    library's allocation: checkpoints of 36 N + 3 G floats; slots of 1,876 E + 6 G floats
+    with attenuation (15 fields of 125 nodes per element, padded to 16 bytes), 1,128 E + 6 G
+    without."""
     N, G = points(elements)
+    E = N / 125
     ckpt = (36 * N + 3 * G) * 4
-    slot = ((15 if is_diss else 9) * N + 6 * G) * 4
+    slot = ((1876 if is_diss else 1128) * E + 6 * G) * 4
     if K2:
         return math.ceil(nt / K) * ckpt + (math.ceil(K / K2) - 1) * ckpt + K2 * slot
     return math.ceil(nt / K) * ckpt + K * slot
