@@ -361,7 +361,7 @@ int ses3d_gpu_exact_gradient(ses3d_gpu *h, int which, double *out, int device);
 int ses3d_gpu_exact_get_field(ses3d_gpu *h, int event, int field, float *out);
 int ses3d_gpu_exact_set_field(ses3d_gpu *h, int event, int field, const float *in);
 
-/* Lean plain-forward stepping (adjoint_flag 0 only; off by default). Outside the PML
+/* Lean stepping (off by default). Outside the PML
  * all profiles vanish, so (SOURCE/ses3d_evolution.f90:123-134,208-219) the displacement
  * gradients dxux..dzuy enter no output and the mirror stresses syx, szx, szy stay equal
  * to sxy, sxz, syz. With lean stepping, elements outside the PML read and write neither:
@@ -371,9 +371,15 @@ int ses3d_gpu_exact_set_field(ses3d_gpu *h, int event, int field, const float *i
  * switched off. The displacement gradients outside the PML are not integrated, so once a
  * lean iteration has run, ses3d_gpu_get_field(SES3D_FIELD_DXUX..DZUY) returns
  * SES3D_E_STATE (for the rest of the run, or until that field is set) instead of values
- * the reference would not produce. begin_adjoint switches lean stepping off. On a handle
- * with the exact adjoint enabled the choice cannot change once stepping has started
- * (SES3D_E_STATE). */
+ * the reference would not produce. begin_adjoint switches lean stepping off.
+ * Handles with adjoint_flag 1 or 2 keep the displacement u = sum of dt v (3 G floats more per
+ * event, in checkpoints too): lean record and kernel-correlation iterations take the
+ * displacement gradients outside the PML as the strain-rate proxies of u (equal to their
+ * time integral up to FP32 rounding of the summation order), so the forward run with
+ * records and the adjoint run step lean as well; recomputes of checkpointed records replay
+ * the forward run's choice. On such handles, and with the exact adjoint enabled, the
+ * choice cannot change once stepping has started (SES3D_E_STATE); begin_adjoint starts a
+ * new run. */
 int ses3d_gpu_set_lean(ses3d_gpu *h, int enable);
 
 /* Element-kernel block shape: elements per CTA (1, 2 or 4); 0 selects the default.

@@ -117,6 +117,8 @@ class MisfitSetup:
     grad_q: bool = True
     exact: bool = False          # backward = exact discrete adjoint of the time stepping
     checkpoint_steps: Optional[int] = None  # exact: forward iterations per checkpoint (None: planned)
+    lean: bool = True            # reference kernels: forward and adjoint runs step lean (displacement
+                                 # gradients outside the PML from the displacement, on stored iterations)
     last: dict = field(default_factory=dict)
 
     @classmethod
@@ -157,8 +159,9 @@ class MisfitSetup:
             sim.set_source(slot, e.xxs, e.yys, e.zzs, e.source_type, e.mom, e.stf)
             sim.set_receivers(slot, e.recloc)
         sim.use_graph(True, 10)   # plain iterations (between stored ones) replay from CUDA graphs
-        if not adjoint:
-            sim.set_lean(True)        # seismograms only: the displacement gradients enter nothing
+        # lean stepping: outside the PML no displacement gradients are kept; seismograms do not
+        # need them and records take them from the displacement
+        sim.set_lean(self.lean or not adjoint)
         if adjoint:
             if K is None:
                 pl = self.plan()
@@ -285,9 +288,10 @@ class MisfitSetup:
         nt, smp = int(c.nt), self.samp_ad
         nrec = len([it for it in range(1, nt + 1) if it % smp == 0 or it == 1 or it == nt])
         shared = 64.0 * N + 12.0 * G
-        event = (36.0 * N + 3.0 * G + 3.0 * N) * 4 + 64.0 * N
+        # per event: element state, velocity and displacement, element forces, FP64 kernels
+        event = (36.0 * N + 6.0 * G + 3.0 * N) * 4 + 64.0 * N
         rec = 36.0 * N
-        ckpt = (36.0 * N + 3.0 * G) * 4
+        ckpt = (36.0 * N + 6.0 * G) * 4
         K = max(1, int(round(math.sqrt(nrec * ckpt / rec))))
         one = event + ckpt + math.ceil(nrec / K) * ckpt + K * rec
         best = None
@@ -484,6 +488,7 @@ class _Misfit:
                         for slot, k in enumerate(grp):
                             sim.set_adjoint_sources(slot, setup.events[k].recloc, srcs[slot])
                         sim.begin_adjoint()
+                        sim.set_lean(setup.lean)
                         sim.run()
                         ksum = kernel_sums_device(sim, rho.device, ksum)   # events in index order
                         sim.close()
@@ -555,6 +560,7 @@ class _Misfit:
                     for k, e in enumerate(setup.events):
                         sim.set_adjoint_sources(k, e.recloc, srcs[k])
                     sim.begin_adjoint()
+                    sim.set_lean(setup.lean)
                     sim.run()
                     ksum = kernel_sums_device(sim, Q.device)
                     sim.close()

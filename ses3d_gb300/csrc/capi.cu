@@ -109,6 +109,9 @@ struct ses3d_gpu {
   float *d_MM = nullptr, *d_mat = nullptr, *d_gmat = nullptr;
   float *d_state = nullptr, *d_v = nullptr, *d_f = nullptr;
   bool state_zero = false;  // d_state holds zeros only (since zero_wavefield, before any step or field write)
+  bool has_u = false;       // runs with records or kernel correlation (adjoint_flag 1, 2): d_v and d_v2
+                            // hold the displacement [nev][3][G] after the velocity
+  bool fwd_lean = false;    // the forward run with records stepped lean (its recomputes do too)
   int *d_aniso = nullptr;   // set by the model derivation when A, B or C is non-zero
   int *d_it = nullptr;
   int *d_err = nullptr;  // device error word (bounded waits)
@@ -393,10 +396,16 @@ int set_model_common(ses3d_gpu *h, const float *const rec[7]) {
   return SES3D_OK;
 }
 
+// Floats of the velocity allocation: the velocity of every event, and the displacement after
+// it on handles that keep one.
+size_t v_floats(const ses3d_gpu *h) {
+  return (size_t)h->cfg.n_events * 3 * (size_t)h->geo.G * (h->has_u ? 2 : 1);
+}
+
 int zero_wavefield(ses3d_gpu *h) {
   const size_t nev = h->cfg.n_events;
   CK(h, cudaMemsetAsync(h->d_state, 0, nev * NSTATE * h->geo.N * sizeof(float), h->st));
-  CK(h, cudaMemsetAsync(h->d_v, 0, nev * 3 * h->geo.G * sizeof(float), h->st));
+  CK(h, cudaMemsetAsync(h->d_v, 0, v_floats(h) * sizeof(float), h->st));
   CK(h, cudaMemsetAsync(h->d_f, 0, nev * 3 * h->geo.N * sizeof(float), h->st));
   CK(h, cudaMemsetAsync(h->d_it, 0, sizeof(int), h->st));
   if (h->d_seis) CK(h, cudaMemsetAsync(h->d_seis, 0, (size_t)3 * h->cfg.nt * h->R * sizeof(float), h->st));
@@ -459,6 +468,7 @@ int launch_iteration(ses3d_gpu *h, const Wave &w, int mode, float *rec, bool tim
   h->state_zero = false;
   p.state = w.state;
   p.v = w.v;
+  p.u = h->has_u ? w.v + (size_t)h->cfg.n_events * 3 * h->geo.G : nullptr;
   p.d_it = w.d_it;
   p.rec = rec;
   p.src_elem = w.adjoint ? h->d_src_none : h->d_src_elem;
@@ -486,9 +496,10 @@ int launch_iteration(ses3d_gpu *h, const Wave &w, int mode, float *rec, bool tim
   return SES3D_OK;
 }
 
-// Floats of one full-state checkpoint (all events): element state and assembled velocity.
+// Floats of one full-state checkpoint (all events): element state, assembled velocity and,
+// where kept, the displacement.
 size_t ckpt_floats(const ses3d_gpu *h) {
-  return (size_t)h->cfg.n_events * ((size_t)NSTATE * h->geo.N + 3 * (size_t)h->geo.G);
+  return (size_t)h->cfg.n_events * (size_t)NSTATE * h->geo.N + v_floats(h);
 }
 
 int save_checkpoint(ses3d_gpu *h, int completed_it) {
@@ -499,8 +510,7 @@ int save_checkpoint(ses3d_gpu *h, int completed_it) {
   h->ckpts.push_back(c);
   h->ckpt_it.push_back(completed_it);
   CK(h, cudaMemcpyAsync(c, h->d_state, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
-  CK(h, cudaMemcpyAsync(c + ns, h->d_v, (size_t)h->cfg.n_events * 3 * h->geo.G * sizeof(float),
-                        cudaMemcpyDeviceToDevice, h->st));
+  CK(h, cudaMemcpyAsync(c + ns, h->d_v, v_floats(h) * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
   return SES3D_OK;
 }
 
@@ -524,7 +534,7 @@ int save_exact_checkpoint(ses3d_gpu *h, int completed_it) {
 int ensure_wave2(ses3d_gpu *h) {
   if (h->d_state2) return SES3D_OK;
   CK(h, dalloc(&h->d_state2, (size_t)h->cfg.n_events * NSTATE * h->geo.N));
-  CK(h, dalloc(&h->d_v2, (size_t)h->cfg.n_events * 3 * h->geo.G));
+  CK(h, dalloc(&h->d_v2, v_floats(h)));
   CK(h, dalloc(&h->d_it2, 1));
   return SES3D_OK;
 }
@@ -532,7 +542,7 @@ int ensure_wave2(ses3d_gpu *h) {
 // Loads a full-state checkpoint (completed iterations it0) into the second wavefield.
 int load_wave2(ses3d_gpu *h, const float *ckpt, const int &it0) {
   const size_t ns = (size_t)h->cfg.n_events * NSTATE * h->geo.N;
-  const size_t nv = (size_t)h->cfg.n_events * 3 * h->geo.G;
+  const size_t nv = v_floats(h);
   int rc = ensure_wave2(h);
   if (rc) return rc;
   CK(h, cudaMemcpyAsync(h->d_state2, ckpt, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
@@ -541,9 +551,18 @@ int load_wave2(ses3d_gpu *h, const float *ckpt, const int &it0) {
   return SES3D_OK;
 }
 
+// Recomputes of the forward run step as it did (lean or full state) while this is in scope.
+struct ForwardStepping {
+  ses3d_gpu *h;
+  int saved;
+  explicit ForwardStepping(ses3d_gpu *hh) : h(hh), saved(hh->c.lean) { h->c.lean = h->fwd_lean ? 1 : 0; }
+  ~ForwardStepping() { h->c.lean = saved; }
+};
+
 // Runs the second wavefield from completed iteration it0 and stores records rA .. rB - 1
 // into segbuf[0 ..] (record iterations in MODE 1, the others plain).
 int recompute_records(ses3d_gpu *h, int it0, int rA, int rB) {
+  ForwardStepping fs(h);
   const size_t rec_floats = (size_t)h->cfg.n_events * NREC * h->geo.N;
   if (!h->d_state2) return fail(h, SES3D_E_STATE, "the recomputing wavefield is not loaded");
   while ((int)h->segbuf.size() < rB - rA) {
@@ -586,11 +605,12 @@ int recompute_segment(ses3d_gpu *h, int s) {
 // starts at the segment's own checkpoint).
 int recompute_level2(ses3d_gpu *h, int s) {
   Range range_("ses3d recompute checkpoints");
+  ForwardStepping fs(h);
   const int r0 = s * h->ckpt_K;
   const int r1 = std::min((int)h->store_steps.size(), r0 + h->ckpt_K);
   const int nsub = (r1 - r0 + h->ckpt_K2 - 1) / h->ckpt_K2;
   const size_t ns = (size_t)h->cfg.n_events * NSTATE * h->geo.N;
-  const size_t nv = (size_t)h->cfg.n_events * 3 * h->geo.G;
+  const size_t nv = v_floats(h);
   while ((int)h->ckpt2.size() < nsub - 1) {
     float *c = nullptr;
     CK(h, dalloc(&c, ckpt_floats(h)));
@@ -807,7 +827,8 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   chk(dalloc(&h->d_aniso, 1));
   chk(dalloc(&h->d_gmat, (size_t)NGMAT * g.N));
   chk(dalloc(&h->d_state, nev * NSTATE * g.N));
-  chk(dalloc(&h->d_v, nev * 3 * g.G));
+  h->has_u = cfg->adjoint_flag >= 1;
+  chk(dalloc(&h->d_v, v_floats(h)));
   chk(dalloc(&h->d_f, nev * 3 * g.N));
   chk(dalloc(&h->d_it, 1));
   chk(dalloc(&h->d_src_elem, nev));
@@ -1093,6 +1114,7 @@ int ses3d_gpu_step(ses3d_gpu *h, int n) {
       int rc = save_exact_checkpoint(h, it - 1);
       if (rc) return rc;
     }
+    if (flag == 1 && it == 1) h->fwd_lean = h->c.lean != 0;
     if (flag == 1 && (it % h->cfg.samp_ad == 0 || it == 1 || it == nt)) {
       if (h->ckpt_K > 0) {  // checkpoint before every ckpt_K-th record, no records kept
         if (h->nrec_done % h->ckpt_K == 0) {
@@ -1413,7 +1435,7 @@ int ses3d_gpu_begin_adjoint(ses3d_gpu *h) {
   if (!h) return SES3D_E_CONFIG;
   h->mode_flag = 2;
   h->cfg.adjoint_flag = 2;
-  h->c.lean = 0;  // lean stepping is a plain-forward mode; the wavefield is zeroed below
+  h->c.lean = 0;  // the adjoint run chooses its own stepping; the wavefield is zeroed below
   if (!h->d_grad) {
     CK(h, dalloc(&h->d_grad, (size_t)h->cfg.n_events * NGRAD * h->geo.N));
   }
@@ -1578,8 +1600,10 @@ int ses3d_gpu_set_checkpoint_levels(ses3d_gpu *h, int records_per_segment, int r
 int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
   if (!h) return 0;
   const size_t N = h->geo.N, G = h->geo.G, nev = h->cfg.n_events;
+  // tables, mass matrix, material, adjoint material; per event the element state and forces;
+  // velocity (and displacement)
   size_t f = (size_t)KTAB_FLOATS + 2 * G + (size_t)ELEM_MAT * h->geo.E + (size_t)NGMAT * N +
-             nev * ((size_t)NSTATE * N + 6 * G);
+             nev * ((size_t)NSTATE * N + 3 * N) + v_floats(h);
   size_t bytes = f * sizeof(float);
   if (h->d_grad) bytes += nev * NGRAD * N * sizeof(double);
   bytes += std::max(h->records.size(), h->record_slots.size()) * nev * NREC * N * sizeof(float);
@@ -1590,14 +1614,17 @@ int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
   bytes += h->ex_slots.size() * nev * ((size_t)slot_stride(h->cfg.is_diss) * h->geo.E + 6 * G) * sizeof(float);
   bytes += h->ex_ckpts2.size() * ckpt_floats(h) * sizeof(float);
   if (h->d_astate) bytes += nev * (((size_t)NSTATE * N + 6 * G + 3 * N) * sizeof(float) + ((size_t)NMAT * N + G) * sizeof(double));
-  if (h->d_state2) bytes += nev * ((size_t)NSTATE * N + 3 * G) * sizeof(float);
+  if (h->d_state2) bytes += (nev * (size_t)NSTATE * N + v_floats(h)) * sizeof(float);
   bytes += (size_t)3 * h->cfg.nt * h->R * sizeof(float);
   return (int64_t)bytes;
 }
 
 int ses3d_gpu_set_lean(ses3d_gpu *h, int enable) {
   if (!h) return SES3D_E_CONFIG;
-  if (enable && h->mode_flag != 0) return fail(h, SES3D_E_CONFIG, "lean stepping applies to plain forward runs only");
+  // A run with records or kernel correlation takes displacement gradients from its state in
+  // PML elements and from the displacement elsewhere: its stepping is chosen before it starts.
+  if (h->mode_flag != 0 && h->it != 0 && (enable != 0) != (h->c.lean != 0))
+    return fail(h, SES3D_E_STATE, "lean stepping of a run with records or kernel correlation is chosen before the run starts");
   // An exact-adjoint run replays its iterations from checkpoints in the same stepping as its
   // forward run, so the choice is made before that run starts and kept.
   if (h->ex_K > 0 && h->it != 0 && (enable != 0) != (h->c.lean != 0))

@@ -61,6 +61,14 @@ __device__ __forceinline__ unsigned force_offset(const Consts &c, int i, int j, 
          (unsigned)(in + 5 * jn + 25 * kn);
 }
 
+// Element-kernel modes: 0 plain, 1 forward record, 2 kernel correlation, in full state; 3,
+// 4, 5 the same lean: outside the PML neither displacement gradients nor mirror stresses
+// are kept, and record and correlation iterations there take the displacement gradients
+// from the displacement field u (both are the time integral of the same linear map of v).
+__host__ __device__ constexpr bool lean_mode(int m) { return m >= 3; }
+__host__ __device__ constexpr bool record_mode(int m) { return m == 1 || m == 4; }
+__host__ __device__ constexpr bool corr_mode(int m) { return m == 2 || m == 5; }
+
 struct NoHook {
   __device__ void operator()() const {}
 };
@@ -80,6 +88,52 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
   const float vx = x.vx, vy = x.vy, vz = x.vz;
   const float clam = x.clam, c2mut = x.c2mut, c2mt = x.c2mt, cA = x.cA, cB2 = x.cB2, cC = x.cC;
   (void)j;
+  // Record or correlation iteration, lean, outside the PML: the displacement gradients at the
+  // end of the iteration are the strain-rate proxies (ses3d_evolution.f90:57-103) of the
+  // displacement u + dt v, by the same contraction through shared memory (s_p is free until
+  // the stress phase); every thread of the CTA takes part (one item per CTA in these modes).
+  float du[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if constexpr (MODE == 4 || MODE == 5) {
+    if (!full) {
+      const float dtu = c.dt;
+      float ux = 0.f, uy = 0.f, uz = 0.f;
+      if (act) {
+        const size_t g =
+            (size_t)(ii * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
+        const float *U = p.u + (size_t)ev * 3 * c.G + g;
+        ux = __fadd_rn(U[0], __fmul_rn(dtu, vx));
+        uy = __fadd_rn(U[c.G], __fmul_rn(dtu, vy));
+        uz = __fadd_rn(U[2 * c.G], __fmul_rn(dtu, vz));
+      }
+      s_p[0][n] = ux; s_p[1][n] = uy; s_p[2][n] = uz;
+      __syncthreads();
+      if (act) {
+        float dxx = 0.f, dxy = 0.f, dxz = 0.f, dyx = 0.f, dyy = 0.f, dyz = 0.f, dzx = 0.f, dzy = 0.f, dzz = 0.f;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+          const int ix = q + 5 * jn + 25 * kn, iy = in + 5 * q + 25 * kn, iz = in + 5 * jn + 25 * q;
+          const float dxq = tab.Dx[in][q], dyq = tab.Dy[jn][q], dzq = tab.Dz[kn][q];
+          dxx = fmaf(s_p[0][ix], dxq, dxx); dxy = fmaf(s_p[1][ix], dxq, dxy); dxz = fmaf(s_p[2][ix], dxq, dxz);
+          dyx = fmaf(s_p[0][iy], dyq, dyx); dyy = fmaf(s_p[1][iy], dyq, dyy); dyz = fmaf(s_p[2][iy], dyq, dyz);
+          dzx = fmaf(s_p[0][iz], dzq, dzx); dzy = fmaf(s_p[1][iz], dzq, dzy); dzz = fmaf(s_p[2][iz], dzq, dzz);
+        }
+        const float *lt0 = x.lt;
+        const float ir0 = lt0 ? lt0[LT_IR + kn] : __ldg(p.inv_r + k * 5 + kn);
+        const float irs0 = ir0 * (lt0 ? lt0[LT_ISIN + in] : __ldg(p.inv_sin + ii * 5 + in));
+        const float ct0 = lt0 ? lt0[LT_COT + in] : __ldg(p.cot_x + ii * 5 + in);
+        du[0] = (uz + dxx) * ir0;                  // dxux
+        du[1] = dyy * irs0 + (uz + ux * ct0) * ir0;  // dyuy
+        du[2] = -dzz;                              // dzuz
+        du[3] = dxy * ir0;                         // dxuy
+        du[4] = -uy * ct0 * ir0 + dyx * irs0;      // dyux
+        du[5] = (dxz - ux) * ir0;                  // dxuz
+        du[6] = -dzx;                              // dzux
+        du[7] = -uy * ir0 + dyz * irs0;            // dyuz
+        du[8] = -dzy;                              // dzuy
+      }
+      __syncthreads();  // s_p read before the stress phase writes it
+    }
+  }
   float r = 1.f, st = 1.f;
   if (act) {
     // strain-rate proxies (ses3d_evolution.f90:57-87)
@@ -119,7 +173,7 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
     // Lean iterations in elements outside the PML: every profile there is zero and the taper
     // one, so the displacement gradients enter nothing and the PML strain terms add zeros;
     // both are skipped (the strain rates keep their values).
-    const bool pml_free = MODE == 3 && !full;
+    const bool pml_free = lean_mode(MODE) && !full;
     float dxux = 0.f, dyuy = 0.f, dzuz = 0.f, dxuy = 0.f, dyux = 0.f, dxuz = 0.f, dzux = 0.f, dyuz = 0.f, dzuy = 0.f;
     float px = 0.f, py = 0.f, pz = 0.f, taper = 1.f;
     if (!pml_free) {
@@ -156,6 +210,12 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
       ezx = ezx + (px + py) * dzux;
       eyz = eyz + (px + pz) * dyuz;
       ezy = ezy + (px + py) * dzuy;
+    }
+    if constexpr (MODE == 4 || MODE == 5) {
+      if (pml_free) {
+        dxux = du[0]; dyuy = du[1]; dzuz = du[2]; dxuy = du[3]; dyux = du[4];
+        dxuz = du[5]; dzux = du[6]; dyuz = du[7]; dzuy = du[8];
+      }
     }
     // symmetrisation (ses3d_evolution.f90:136-138)
     exy = (exy + eyx) * 0.5f;
@@ -225,7 +285,7 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
     S[F_SXY * 125] = s_xy * taper; S[F_SXZ * 125] = s_xz * taper; S[F_SYZ * 125] = s_yz * taper;
     if (full) { S[F_SYX * 125] = s_yx * taper; S[F_SZX * 125] = s_zx * taper; S[F_SZY * 125] = s_zy * taper; }
     // moment-tensor source field (ses3d_miscellaneous.f90:115-147)
-    if (MODE != 2 && (int)e == (lt ? __float_as_int(lt[LT_SRC]) : __ldg(p.src_elem + ev))) {
+    if (!corr_mode(MODE) && (int)e == (lt ? __float_as_int(lt[LT_SRC]) : __ldg(p.src_elem + ev))) {
       const int it = *p.d_it + 1;
       const float d = p.src_delta[ev * 125 + nn];
       const float so = p.stf[(size_t)ev * c.nt + (it - 1)];
@@ -242,13 +302,13 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
     s_p[3][n] = wy * s_yx; s_p[4][n] = wy * s_yy; s_p[5][n] = wy * s_yz;
     s_p[6][n] = wz * s_zx; s_p[7][n] = wz * s_zy; s_p[8][n] = wz * s_zz;
 
-    if (MODE == 1) {  // forward record (ses3d_main.f90:148-158)
+    if (record_mode(MODE)) {  // forward record (ses3d_main.f90:148-158)
       float *R = p.rec + (size_t)ev * NREC * N + m0;
       R[R_VX * N] = vx; R[R_VY * N] = vy; R[R_VZ * N] = vz;
       R[R_EXX * N] = dxux; R[R_EYY * N] = dyuy; R[R_EZZ * N] = dzuz;
       R[R_EXY * N] = (dxuy + dyux) * 0.5f; R[R_EXZ * N] = (dxuz + dzux) * 0.5f; R[R_EYZ * N] = (dyuz + dzuy) * 0.5f;
     }
-    if (MODE == 2 && p.rec) {  // kernel correlation (ses3d_grad.f90:53-83, ses3d_grad_Q.f90:111-143)
+    if (corr_mode(MODE) && p.rec) {  // kernel correlation (ses3d_grad.f90:53-83, ses3d_grad_Q.f90:111-143)
       const float *R = p.rec + (size_t)ev * NREC * N + m0;
       const float vxf = R[R_VX * N], vyf = R[R_VY * N], vzf = R[R_VZ * N];
       const float exxf = R[R_EXX * N], eyyf = R[R_EYY * N], ezzf = R[R_EZZ * N];
@@ -328,6 +388,7 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
 // ---------------------------------------------------------------------------------------
 template <bool DISS, int MODE, int EPB>
 __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_ELEM_MINB / EPB : 1)) k_element(const Consts c, const Ptrs p) {
+  static_assert(MODE <= 3, "lean record and correlation iterations run the persistent kernel");
   __shared__ KTab tab;
   __shared__ float s_v[EPB][3][TPE];
   __shared__ float s_p[EPB][9][TPE];
@@ -457,13 +518,13 @@ __device__ __forceinline__ void issue_item(const Consts &c, const Ptrs &p, long 
   const char *msrc = reinterpret_cast<const char *>(p.mat + (size_t)e * ELEM_MAT);
   char *dst = reinterpret_cast<char *>(st->state);
   const unsigned MB = (c.iso ? 3 * MAT_ROW : ELEM_MAT) * (unsigned)sizeof(float);
-  if (!DISS && MODE == 3 && !in_pml_element(c, i, j, k)) {
+  if (!DISS && lean_mode(MODE) && !in_pml_element(c, i, j, k)) {
     mbar_arrive_expect_tx(bar, 3008u + MB);
     bulk_g2s(dst, src, 3008u, bar);
   } else if (!DISS) {
     mbar_arrive_expect_tx(bar, 9008u + MB);
     bulk_g2s(dst, src, 9008u, bar);
-  } else if (MODE == 3 && !in_pml_element(c, i, j, k)) {
+  } else if (lean_mode(MODE) && !in_pml_element(c, i, j, k)) {
     mbar_arrive_expect_tx(bar, 3008u + 9008u + MB);
     bulk_g2s(dst, src, 3008u, bar);
     bulk_g2s(dst + 8992, src + 8992, 9008u, bar);
@@ -541,7 +602,7 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
   const bool on = n < 125;
   const int nn = on ? n : 0;
   const int in = nn % 5, jn = (nn / 5) % 5, kn = nn / 25;
-  constexpr bool TABLES = MODE == 3;
+  constexpr bool TABLES = lean_mode(MODE);
   if (TMA_VBUF == 2 && first < total) gather_v_async<TABLES>(c, p, first, s_vb, s_lt, n, in, jn, kn);
   for (int t = 0;; ++t) {
     const long long item = first + (long long)t * stride;
@@ -553,7 +614,7 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
     const unsigned e = (unsigned)(item / c.nev);
     const int i = (int)(e % (unsigned)c.ex), j = (int)((e / (unsigned)c.ex) % (unsigned)c.ey);
     const int k = (int)(e / ((unsigned)c.ex * (unsigned)c.ey));
-    const bool full = MODE != 3 || in_pml_element(c, i, j, k);
+    const bool full = !lean_mode(MODE) || in_pml_element(c, i, j, k);
     float vx = 0.f, vy = 0.f, vz = 0.f;
     if (TMA_VBUF == 2) {  // this item's velocity was gathered one item ahead
       asm volatile("cp.async.wait_group 0;" ::: "memory");
@@ -626,7 +687,7 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
     // short, so right after this item's state has been read; full-state items after the
     // stress/divergence barrier, which keeps thread 0's copy work off that barrier
     // (2.65 -> 2.42 ms per launch), while lean iterations lose 6 % that way.
-    constexpr bool LATE_REFILL = (MODE != 3) != (REFILL == 1);
+    constexpr bool LATE_REFILL = (!lean_mode(MODE)) != (REFILL == 1);
     if (!LATE_REFILL) issue_refill();
     const size_t m0 = (size_t)e * 125 + nn;
     float *S = p.state + ((size_t)ev * c.E + e) * ELEM_STATE + nn;
@@ -643,9 +704,10 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
 // ses3d_evolution.f90:286-310), then a = s / MM, v += dt (a - prof v), v *= taper
 // (ses3d_evolution.f90:318-328,366).
 // ---------------------------------------------------------------------------------------
-// STORE_F: also write the assembled forces (a run whose states the exact adjoint replays).
+// KIND 1: also write the assembled forces (a run whose states the exact adjoint replays);
+// KIND 2: also integrate the displacement, u += dt v with the velocity before the update.
 // TPB threads per CTA, MINB resident CTAs per SM requested from ptxas.
-template <bool STORE_F, int TPB = SES3D_NODE_TPB, int MINB = SES3D_NODE_MINB>
+template <int KIND, int TPB = SES3D_NODE_TPB, int MINB = SES3D_NODE_MINB>
 __global__ void __launch_bounds__(TPB, MINB) k_node(const Consts c, const Ptrs p) {
   const int gz = blockIdx.y, ev = blockIdx.z;
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
@@ -667,9 +729,15 @@ __global__ void __launch_bounds__(TPB, MINB) k_node(const Consts c, const Ptrs p
   const float pxr = __ldg(p.pxg + gx), pyr = __ldg(p.pyg + gy), pzr = __ldg(p.pzg + gz);
   float sx, sy, sz;
   gather_node(c, p.f + (size_t)ev * 3 * (size_t)c.N, gx, gy, gz, sx, sy, sz);
-  if (STORE_F) {
+  if (KIND == 1) {
     float *Fo = p.fg + (size_t)ev * 3 * c.G + g;
     Fo[0] = sx; Fo[c.G] = sy; Fo[2 * c.G] = sz;
+  }
+  if (KIND == 2) {  // the element kernel forms the same sums for its record iterations
+    float *U = p.u + (size_t)ev * 3 * c.G + g;
+    U[0] = __fadd_rn(U[0], __fmul_rn(c.dt, vx));
+    U[c.G] = __fadd_rn(U[c.G], __fmul_rn(c.dt, vy));
+    U[2 * c.G] = __fadd_rn(U[2 * c.G], __fmul_rn(c.dt, vz));
   }
   // a = s / MM with the reciprocal of the mass matrix (ses3d_evolution.f90:318-320)
   const float ax = sx * imm, ay = sy * imm, az = sz * imm;
@@ -1080,6 +1148,10 @@ cudaError_t prepare_element_kernels() {
   if ((e = prepare_tma<false, 2, 0>()) != cudaSuccess) return e;
   if ((e = prepare_tma<true, 1, 0>()) != cudaSuccess) return e;
   if ((e = prepare_tma<true, 2, 0>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<false, 4, 1>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<false, 5, 1>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<true, 4, 1>()) != cudaSuccess) return e;
+  if ((e = prepare_tma<true, 5, 1>()) != cudaSuccess) return e;
   if ((e = prepare_tma<false, 0, 0, true>()) != cudaSuccess) return e;
   if ((e = prepare_tma<false, 3, 0, true>()) != cudaSuccess) return e;
   if ((e = prepare_tma<true, 0, 0, true>()) != cudaSuccess) return e;
@@ -1117,8 +1189,16 @@ int element_shape_count() { return kTmaShapes; }
 // 0 (they are one iteration in samp_ad; the searched shapes serve the plain iterations).
 // With p.slot set (plain or lean iterations), the persistent kernel in shape 0 also packs
 // each item's starting state into the slot, whatever epb and shape say.
+// Lean handles map modes 0, 1, 2 to 3, 4, 5; modes 4 and 5 (they need p.u) run the
+// persistent kernel in shape 1 (4 CTAs per SM: their displacement contraction needs the
+// registers).
 cudaError_t launch_element(int diss, int mode, int epb, int shape, const Consts &c, const Ptrs &p, cudaStream_t st) {
-  if (mode == 0 && c.lean) mode = 3;
+  if (c.lean && mode <= 2) mode += 3;
+  if (mode == 4 || mode == 5) {
+    if (!p.u) return cudaErrorInvalidValue;
+    if (mode == 4) return diss ? launch_tma<true, 4, 1>(c, p, st) : launch_tma<false, 4, 1>(c, p, st);
+    return diss ? launch_tma<true, 5, 1>(c, p, st) : launch_tma<false, 5, 1>(c, p, st);
+  }
   if (p.slot) {
     if (mode == 0) return diss ? launch_tma<true, 0, 0, true>(c, p, st) : launch_tma<false, 0, 0, true>(c, p, st);
     if (mode == 3) return diss ? launch_tma<true, 3, 0, true>(c, p, st) : launch_tma<false, 3, 0, true>(c, p, st);
@@ -1142,25 +1222,28 @@ cudaError_t launch_element(int diss, int mode, int epb, int shape, const Consts 
   return launch_elem_epb<false, 0>(epb, c, p, st);
 }
 
-template <bool STORE_F, int TPB, int MINB>
+template <int KIND, int TPB, int MINB>
 static cudaError_t launch_node_tpb(const Consts &c, const Ptrs &p, cudaStream_t st) {
   dim3 grid((unsigned)(((long long)c.GX * c.GY + TPB - 1) / TPB), (unsigned)c.GZ, (unsigned)c.nev);
-  k_node<STORE_F, TPB, MINB><<<grid, TPB, 0, st>>>(c, p);
+  k_node<KIND, TPB, MINB><<<grid, TPB, 0, st>>>(c, p);
   return cudaGetLastError();
 }
 
 // node_block: threads per CTA of the node kernel, 128, 256 (default) or 512, each with the
 // resident CTAs per SM that fill 1,536-1,792 thread slots.
-template <bool STORE_F>
+template <int KIND>
 static cudaError_t launch_node_shape(int node_block, const Consts &c, const Ptrs &p, cudaStream_t st) {
-  if (node_block == 128) return launch_node_tpb<STORE_F, 128, 14>(c, p, st);
-  if (node_block == 512) return launch_node_tpb<STORE_F, 512, 3>(c, p, st);
-  return launch_node_tpb<STORE_F, SES3D_NODE_TPB, SES3D_NODE_MINB>(c, p, st);
+  if (node_block == 128) return launch_node_tpb<KIND, 128, 14>(c, p, st);
+  if (node_block == 512) return launch_node_tpb<KIND, 512, 3>(c, p, st);
+  return launch_node_tpb<KIND, SES3D_NODE_TPB, SES3D_NODE_MINB>(c, p, st);
 }
 
+// With p.fg the assembled forces are stored too; with p.u the displacement is integrated.
 cudaError_t launch_node(int node_block, const Consts &c, const Ptrs &p, cudaStream_t st) {
-  if (p.fg) return launch_node_shape<true>(node_block, c, p, st);
-  return launch_node_shape<false>(node_block, c, p, st);
+  if (p.fg && p.u) return cudaErrorInvalidValue;
+  if (p.fg) return launch_node_shape<1>(node_block, c, p, st);
+  if (p.u) return launch_node_shape<2>(node_block, c, p, st);
+  return launch_node_shape<0>(node_block, c, p, st);
 }
 
 cudaError_t launch_receivers(const Consts &c, const float *v, const int *rec_elem, const int *rec_ev,

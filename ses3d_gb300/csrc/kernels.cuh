@@ -96,6 +96,8 @@ struct Ptrs {
   float *rec;                           // record of this iteration: [nev][NREC][N]
   double *grad;                         // [nev][NGRAD][N]
   int grad_q;                           // accumulate the Q kernels too
+  float *u;                             // [nev][3][G] displacement (time integral of v) of runs that
+                                        // store records or correlate kernels lean, or null
   float *slot;                          // [nev][E][slot_stride]: the iteration's starting state,
                                         // packed for the exact adjoint, or null
 };

@@ -54,6 +54,20 @@ def runs(native, oracle_mod, problem):
     out["gpu_kernels"] = {k: sim.kernel(k) for k in ("rho", "cp", "csh", "csv", "Q_mu", "alpha_mu", "Q_kappa")}
     out["gpu_is"] = sim.setup_int("is")
     sim.close()
+    # the same runs stepped lean: records and correlations outside the PML take the
+    # displacement gradients from the displacement
+    lean = Simulation.from_problem(p, adjoint_flag=1, grad_variant=1)
+    lean.set_lean(True)
+    lean.run()
+    out["lean_records"] = [lean.record(r) for r in range(lean.record_count())]
+    out["lean_seis"] = lean.seismograms(0)
+    lean.set_adjoint_sources(0, loc, stf)
+    lean.begin_adjoint()
+    lean.set_lean(True)
+    lean.run()
+    out["lean_kernels"] = {k: lean.kernel(k) for k in ("rho", "cp", "csh", "csv", "Q_mu", "alpha_mu", "Q_kappa")}
+    lean.close()
+    out["gpu_seis"] = gseis
     for fp64 in (False, True):
         o = oracle_mod.Oracle(p, fp64=fp64, adjoint_flag=1)
         o.run(NT)
@@ -73,8 +87,9 @@ def runs(native, oracle_mod, problem):
     return out
 
 
+@pytest.mark.parametrize("lean", [False, True])
 @pytest.mark.parametrize("K,K2", [(1, 0), (3, 0), (100, 0), (5, 2), (12, 5), (4, 3)])
-def test_checkpointed_records_give_identical_kernels(native, problem, runs, K, K2):
+def test_checkpointed_records_give_identical_kernels(native, problem, runs, K, K2, lean):
     """Checkpoints every K records + segment recompute (K2 = 0), or two levels (segments of
     K records recomputed into checkpoints every K2 records, sub-segments recomputed from
     those) = keeping every record, bit for bit."""
@@ -83,6 +98,7 @@ def test_checkpointed_records_give_identical_kernels(native, problem, runs, K, K
     p = problem
     sim = Simulation.from_problem(p, adjoint_flag=1, grad_variant=1)
     _lib.check(sim.lib.ses3d_gpu_set_checkpoint_levels(sim.h, K, K2), sim.h)
+    sim.set_lean(lean)
     sim.run()
     assert sim.record_count() == len(runs["gpu_records"])
     assert np.array_equal(sim.saving_vector(), runs["gpu_sv"])
@@ -90,9 +106,11 @@ def test_checkpointed_records_give_identical_kernels(native, problem, runs, K, K
     loc, stf = adjoint_inputs(p, gseis)
     sim.set_adjoint_sources(0, loc, stf)
     sim.begin_adjoint()
+    sim.set_lean(lean)
     sim.run()
+    ref = runs["lean_kernels" if lean else "gpu_kernels"]
     for k in ("rho", "cp", "csh", "csv", "Q_mu"):
-        assert np.array_equal(sim.kernel(k), runs["gpu_kernels"][k]), k
+        assert np.array_equal(sim.kernel(k), ref[k]), k
     sim.close()
 
 
@@ -104,14 +122,45 @@ def test_checkpoint_levels_rejects_bad_lengths(native, problem):
         assert sim.lib.ses3d_gpu_set_checkpoint_levels(sim.h, 4, 2) == 0
 
 
+def test_lean_records_and_kernels_follow_full_state(runs):
+    """Lean runs with records: the same seismograms bit for bit, records and kernels equal
+    to the full-state run's within FP32 rounding (outside the PML the displacement gradients
+    are the strain-rate proxies of the displacement, summed in another order)."""
+    for a, b in zip(runs["lean_seis"], runs["gpu_seis"]):
+        assert np.abs(b).max() > 0 and np.array_equal(a, b)
+    for r, (a, b) in enumerate(zip(runs["lean_records"], runs["gpu_records"])):
+        for f in range(9):
+            if np.abs(b[f]).max() == 0:
+                continue
+            assert rel(a[f], b[f]) <= 2e-5, (r, f, rel(a[f], b[f]))
+    for k, b in runs["gpu_kernels"].items():
+        assert rel(runs["lean_kernels"][k], b) <= 1e-4, (k, rel(runs["lean_kernels"][k], b))
+
+
+def test_lean_choice_is_fixed_once_a_run_with_records_starts(native, problem):
+    from ses3d_gb300 import _lib
+    from ses3d_gb300.solver import Simulation
+    with Simulation.from_problem(problem, adjoint_flag=1) as sim:
+        sim.set_lean(True)
+        sim.step(3)
+        assert sim.lib.ses3d_gpu_set_lean(sim.h, 0) == -4
+        assert sim.lib.ses3d_gpu_set_lean(sim.h, 1) == 0
+        with pytest.raises(_lib.Ses3dError):
+            sim.field("dxux")
+        sim.run()
+        sim.begin_adjoint()
+        assert sim.lib.ses3d_gpu_set_lean(sim.h, 0) == 0   # a new run: free to choose again
+
+
 def test_saving_vector(runs):
     assert np.array_equal(runs["gpu_sv"], runs["o_sv32"])
     expected = [it if (it % SAMP == 0 or it == 1 or it == NT) else 0 for it in range(1, NT + 1)]
     assert list(runs["gpu_sv"]) == expected
 
 
-def test_records(runs):
-    g, o = runs["gpu_records"], runs["o_records64"]
+@pytest.mark.parametrize("which", ["gpu_records", "lean_records"])
+def test_records(runs, which):
+    g, o = runs[which], runs["o_records64"]
     assert len(g) == len(o)
     for r in range(len(g)):
         for f in range(9):
@@ -126,18 +175,20 @@ def test_adjoint_source_location_bit_exact(runs):
     assert np.array_equal(runs["gpu_is"], runs["o_is32"][: 3 * runs["nad"]])
 
 
+@pytest.mark.parametrize("which", ["gpu_kernels", "lean_kernels"])
 @pytest.mark.parametrize("name", ["rho", "cp", "csh", "csv"])
-def test_kernels(runs, name):
-    g = runs["gpu_kernels"][name]
+def test_kernels(runs, name, which):
+    g = runs[which][name]
     o64 = runs["o_kernels64"][name]
     o32 = runs["o_kernels32"][name]
     assert np.abs(o64).max() > 0
     assert rel(g, o64) <= 1e-3, (name, rel(g, o64), rel(o32, o64))
 
 
+@pytest.mark.parametrize("which", ["gpu_kernels", "lean_kernels"])
 @pytest.mark.parametrize("name", ["Q_mu", "alpha_mu", "Q_kappa"])
-def test_q_kernels(runs, name):
-    g = runs["gpu_kernels"][name]
+def test_q_kernels(runs, name, which):
+    g = runs[which][name]
     o64 = runs["o_kernels64"][name]
     assert np.abs(o64).max() > 0
     assert rel(g, o64) <= 1e-3, (name, rel(g, o64))

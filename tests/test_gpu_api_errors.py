@@ -69,15 +69,18 @@ def test_rejected_calls_leave_the_handle_usable(native):
 
 
 def test_adjoint_handle_rejections(native):
-    """Lean stepping is refused in a flag-1 run; records are refused once checkpointing
-    replaces them; external stepping needs a 16-byte aligned state buffer and a plain run."""
+    """Lean stepping of a flag-1 run is chosen before it starts and cannot change during it;
+    records are refused once checkpointing replaces them; external stepping needs a 16-byte
+    aligned state buffer and a plain run."""
     import torch
     from ses3d_gb300.solver import Simulation
     p = synth.make_problem("tiny", nt=20, seed=62, adjoint_flag=1)
     with Simulation.from_problem(p, adjoint_flag=1) as sim:
-        assert native.ses3d_gpu_set_lean(sim.h, 1) == CONFIG
-        assert b"plain forward" in native.ses3d_gpu_last_error(sim.h)
+        assert native.ses3d_gpu_set_lean(sim.h, 1) == 0
         assert native.ses3d_gpu_set_checkpointing(sim.h, 4) == 0
+        sim.step(2)
+        assert native.ses3d_gpu_set_lean(sim.h, 0) == STATE
+        assert b"chosen before the run starts" in native.ses3d_gpu_last_error(sim.h)
         sim.run()
         out = np.zeros(sim.N * 9, np.float32)
         assert native.ses3d_gpu_get_record(sim.h, 0, 0, L.fptr(out)) == STATE
