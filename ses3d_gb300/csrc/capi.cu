@@ -160,6 +160,8 @@ struct ses3d_gpu {
   std::vector<float *> ex_ckpts;           // at completed iterations 0, ex_K, 2 ex_K, ...
   std::vector<float *> ex_ckpts2;          // second-level checkpoints of the segment being reversed
   std::vector<float *> ex_slots;
+  std::vector<float *> ex_blocks;          // owned allocations holding ex_ckpts, ex_ckpts2, ex_slots
+  size_t ex_block_floats = 0;
   float *d_astate = nullptr, *d_av = nullptr, *d_aF = nullptr, *d_af = nullptr;
   double *d_egmat = nullptr, *d_egimm = nullptr;
   int *d_ait = nullptr;
@@ -514,17 +516,29 @@ int save_checkpoint(ses3d_gpu *h, int completed_it) {
   return SES3D_OK;
 }
 
+// Grows `views` to `count` buffers of `floats` each (rounded up to 256 bytes), carved from
+// one new allocation: a few large allocations instead of one per buffer.
+int grow_exact_buffers(ses3d_gpu *h, std::vector<float *> &views, size_t count, size_t floats) {
+  if (views.size() >= count) return SES3D_OK;
+  const size_t stride = (floats + 63) & ~(size_t)63;
+  const size_t add = count - views.size();
+  float *block = nullptr;
+  CK(h, dalloc(&block, add * stride));
+  h->ex_blocks.push_back(block);
+  h->ex_block_floats += add * stride;
+  for (size_t q = 0; q < add; ++q) views.push_back(block + q * stride);
+  return SES3D_OK;
+}
+
 // Full-state checkpoint of the primary wavefield for the exact adjoint (completed
 // iterations = 0, ex_K, 2 ex_K, ...); kept for the whole run.
 int save_exact_checkpoint(ses3d_gpu *h, int completed_it) {
   const int idx = completed_it / h->ex_K;
   const size_t ns = (size_t)h->cfg.n_events * NSTATE * h->geo.N;
   const size_t nv = (size_t)h->cfg.n_events * 3 * h->geo.G;
-  while ((int)h->ex_ckpts.size() <= idx) {
-    float *c = nullptr;
-    CK(h, dalloc(&c, ckpt_floats(h)));
-    h->ex_ckpts.push_back(c);
-  }
+  const size_t nseg = ((size_t)h->cfg.nt + h->ex_K - 1) / h->ex_K;
+  int rc = grow_exact_buffers(h, h->ex_ckpts, std::max(nseg, (size_t)idx + 1), ckpt_floats(h));
+  if (rc) return rc;
   CK(h, cudaMemcpyAsync(h->ex_ckpts[idx], h->d_state, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
   CK(h, cudaMemcpyAsync(h->ex_ckpts[idx] + ns, h->d_v, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
   return SES3D_OK;
@@ -901,9 +915,7 @@ int ses3d_gpu_destroy(ses3d_gpu *h) {
   for (float *r : h->ckpts) dfree(r);
   for (float *r : h->segbuf) dfree(r);
   for (float *r : h->ckpt2) dfree(r);
-  for (float *r : h->ex_ckpts) dfree(r);
-  for (float *r : h->ex_slots) dfree(r);
-  for (float *r : h->ex_ckpts2) dfree(r);
+  for (float *r : h->ex_blocks) dfree(r);
   free_forces(h->fseis);
   {
     void *ex[] = {h->d_astate, h->d_av, h->d_aF, h->d_af, h->d_egmat, h->d_egimm, h->d_ait};
@@ -1610,9 +1622,7 @@ int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
   bytes += h->ckpts.size() * ckpt_floats(h) * sizeof(float);
   bytes += h->segbuf.size() * nev * NREC * N * sizeof(float);
   bytes += h->ckpt2.size() * ckpt_floats(h) * sizeof(float);
-  bytes += h->ex_ckpts.size() * ckpt_floats(h) * sizeof(float);
-  bytes += h->ex_slots.size() * nev * ((size_t)slot_stride(h->cfg.is_diss) * h->geo.E + 6 * G) * sizeof(float);
-  bytes += h->ex_ckpts2.size() * ckpt_floats(h) * sizeof(float);
+  bytes += h->ex_block_floats * sizeof(float);
   if (h->d_astate) bytes += nev * (((size_t)NSTATE * N + 6 * G + 3 * N) * sizeof(float) + ((size_t)NMAT * N + G) * sizeof(double));
   if (h->d_state2) bytes += (nev * (size_t)NSTATE * N + v_floats(h)) * sizeof(float);
   bytes += (size_t)3 * h->cfg.nt * h->R * sizeof(float);
@@ -1799,17 +1809,11 @@ int ses3d_gpu_exact_backward(ses3d_gpu *h) {
   const int ait0 = nt - 1;
   CK(h, cudaMemcpyAsync(h->d_ait, &ait0, sizeof(int), cudaMemcpyHostToDevice, h->st));
   const int K2 = h->ex_K2 > 0 ? h->ex_K2 : K;  // iterations recomputed into slots at a time
-  while ((int)h->ex_slots.size() < std::min(K2, nt)) {
-    float *q = nullptr;
-    CK(h, dalloc(&q, nsl + 2 * nv));
-    h->ex_slots.push_back(q);
-  }
+  rc = grow_exact_buffers(h, h->ex_slots, (size_t)std::min(K2, nt), nsl + 2 * nv);
+  if (rc) return rc;
   const int nsub_max = (std::min(K, nt) + K2 - 1) / K2;
-  while ((int)h->ex_ckpts2.size() < nsub_max - 1) {
-    float *q = nullptr;
-    CK(h, dalloc(&q, ckpt_floats(h)));
-    h->ex_ckpts2.push_back(q);
-  }
+  rc = grow_exact_buffers(h, h->ex_ckpts2, (size_t)std::max(0, nsub_max - 1), ckpt_floats(h));
+  if (rc) return rc;
   Ptrs p = make_ptrs(h);
   AdjPtrs a;
   std::memset(&a, 0, sizeof(a));
