@@ -377,9 +377,12 @@ int ses3d_gpu_exact_set_field(ses3d_gpu *h, int event, int field, const float *i
  * displacement gradients outside the PML as the strain-rate proxies of u (equal to their
  * time integral up to FP32 rounding of the summation order), so the forward run with
  * records and the adjoint run step lean as well; recomputes of checkpointed records replay
- * the forward run's choice. On such handles, and with the exact adjoint enabled, the
- * choice cannot change once stepping has started (SES3D_E_STATE); begin_adjoint starts a
- * new run. */
+ * the forward run's choice. Such a run must start with zero displacement gradients (a run
+ * from rest, or after begin_adjoint): stepping it lean after ses3d_gpu_set_field set one
+ * returns SES3D_E_STATE. On such handles, and with the exact adjoint enabled, the choice
+ * cannot change once stepping has started (SES3D_E_STATE); begin_adjoint starts a new run.
+ * Every lean run assumes the mirror stresses outside the PML equal their partners, as they
+ * do from rest. */
 int ses3d_gpu_set_lean(ses3d_gpu *h, int enable);
 
 /* Element-kernel block shape: elements per CTA (1, 2 or 4); 0 selects the default.

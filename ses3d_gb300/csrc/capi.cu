@@ -112,6 +112,7 @@ struct ses3d_gpu {
   bool has_u = false;       // runs with records or kernel correlation (adjoint_flag 1, 2): d_v and d_v2
                             // hold the displacement [nev][3][G] after the velocity
   bool fwd_lean = false;    // the forward run with records stepped lean (its recomputes do too)
+  bool du_set = false;      // displacement gradients were set since the wavefield was zeroed
   int *d_aniso = nullptr;   // set by the model derivation when A, B or C is non-zero
   int *d_it = nullptr;
   int *d_err = nullptr;  // device error word (bounded waits)
@@ -415,6 +416,7 @@ int zero_wavefield(ses3d_gpu *h) {
   h->du_stale = 0;
   h->it = 0;
   h->state_zero = true;
+  h->du_set = false;
   return SES3D_OK;
 }
 
@@ -1096,6 +1098,13 @@ int ses3d_gpu_step(ses3d_gpu *h, int n) {
   if (n < 0) return fail(h, SES3D_E_CONFIG, "n must be >= 0");
   if (h->external_stepped)
     return fail(h, SES3D_E_STATE, "this handle steps a caller-owned wavefield (ses3d_gpu_step_external)");
+  // Lean record and correlation iterations add the displacement gradients of the
+  // displacement integrated since the wavefield was zeroed: exact for runs whose
+  // displacement gradients start at zero.
+  if (h->c.lean && h->mode_flag != 0 && h->du_set)
+    return fail(h, SES3D_E_STATE,
+                "lean stepping of a run with records or kernel correlation needs it to start with zero displacement "
+                "gradients; some were set (set_field)");
   const int nt = h->cfg.nt;
   int done = 0;
   while (done < n && h->it < nt) {
@@ -1219,7 +1228,10 @@ static int field_io(ses3d_gpu *h, int event, int field, float *hout, const float
     return fail(h, SES3D_E_STATE,
                 "lean iterations did not integrate this displacement gradient outside the PML (set_lean)");
   const long long N = h->geo.N, G = h->geo.G;
-  if (hin && !adjoint) h->state_zero = false;
+  if (hin && !adjoint) {
+    h->state_zero = false;
+    if (field >= SES3D_FIELD_DXUX && field <= SES3D_FIELD_DZUY) h->du_set = true;
+  }
   float *vbase = (adjoint ? h->d_av : h->d_v) + (size_t)event * 3 * G;
   float *sbase = (adjoint ? h->d_astate : h->d_state) + (size_t)event * NSTATE * N;
   if (field >= SES3D_FIELD_VX_GLOBAL && field <= SES3D_FIELD_VZ_GLOBAL) {

@@ -150,6 +150,17 @@ def test_lean_choice_is_fixed_once_a_run_with_records_starts(native, problem):
         sim.run()
         sim.begin_adjoint()
         assert sim.lib.ses3d_gpu_set_lean(sim.h, 0) == 0   # a new run: free to choose again
+    with Simulation.from_problem(problem, adjoint_flag=1) as sim:
+        # lean records add the gradients of the displacement since the start: a run whose
+        # displacement gradients were set is refused
+        sim.set_field("dxux", np.zeros(sim.N, np.float32))
+        sim.set_lean(True)
+        with pytest.raises(_lib.Ses3dError) as err:
+            sim.step(1)
+        assert err.value.code == -4 and sim.it == 0
+        sim.set_lean(False)
+        sim.step(1)
+        assert sim.it == 1
 
 
 def test_saving_vector(runs):
@@ -292,18 +303,21 @@ def test_graph_replay_in_record_and_adjoint_runs(native, problem, runs, K):
             assert np.array_equal(sim.kernel(k), runs["gpu_kernels"][k]), k
 
 
-def test_elastic_adjoint_kernels_match_oracle(native, oracle_mod):
+@pytest.mark.parametrize("lean", [False, True])
+def test_elastic_adjoint_kernels_match_oracle(native, oracle_mod, lean):
     """is_diss = 0 (no memory variables, the elastic element kernels): forward records and
-    the four elastic Frechet kernels against the FP64 oracle."""
+    the four elastic Frechet kernels against the FP64 oracle, in full state and lean."""
     from ses3d_gb300.solver import Simulation
     p = synth.make_problem("small", nt=NT, seed=33, adjoint_flag=1, is_diss=0)
     p.setup.samp_ad = SAMP
     with Simulation.from_problem(p, adjoint_flag=1) as sim:
+        sim.set_lean(lean)
         sim.run()
         g_rec = [sim.record(r) for r in range(sim.record_count())]
         loc, stf = adjoint_inputs(p, sim.seismograms(0))
         sim.set_adjoint_sources(0, loc, stf)
         sim.begin_adjoint()
+        sim.set_lean(lean)
         sim.run()
         g = {k: sim.kernel(k) for k in ("rho", "cp", "csh", "csv")}
     o = oracle_mod.Oracle(p, fp64=True, adjoint_flag=1)
