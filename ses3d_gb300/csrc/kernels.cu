@@ -969,17 +969,16 @@ __global__ void __launch_bounds__(256) k_derive_blocked(const ModelRecords m, fl
 }
 
 // Element-blocked fields <-> the reference layout, as a 32 x 32 shared-memory transpose:
-// blocked[e * stride + off + n] (n < 125; n < 128 with zero padding) <-> ref[n * E + e].
+// blocked[e * stride + off + n] (n < 125) <-> ref[n * E + e].
 // grid (ceil(E / 32), 4, nfields); field z uses off + z * field_step and ref + z * 125 E.
 __global__ void k_blocked_ref(float *__restrict__ blocked, long long stride, long long off, long long field_step,
-                              float *__restrict__ ref, long long E, int to_ref, int pad) {
+                              float *__restrict__ ref, long long E, int to_ref) {
   __shared__ float tile[32][33];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const long long e0 = (long long)blockIdx.x * 32;
   const int n0 = blockIdx.y * 32;
   float *blk = blocked + off + (long long)blockIdx.z * field_step;
   float *rf = ref + (long long)blockIdx.z * 125 * E;
-  const int nmax = pad ? 128 : 125;
   if (!to_ref) {
     for (int r = ty; r < 32; r += 8) {
       const int n = n0 + r;
@@ -990,7 +989,7 @@ __global__ void k_blocked_ref(float *__restrict__ blocked, long long stride, lon
     for (int r = ty; r < 32; r += 8) {
       const long long e = e0 + r;
       const int n = n0 + tx;
-      if (e < E && n < nmax) blk[e * stride + n] = tile[tx][r];
+      if (e < E && n < 125) blk[e * stride + n] = tile[tx][r];
     }
   } else {
     for (int r = ty; r < 32; r += 8) {
@@ -1323,7 +1322,7 @@ cudaError_t launch_mass(const Consts &c, const float *rhoinv, const float *z, co
 
 cudaError_t launch_state_field(float *state_ev, int field, float *ref, long long E, int to_ref, cudaStream_t st) {
   k_blocked_ref<<<dim3((unsigned)((E + 31) / 32), 4, 1), dim3(32, 8), 0, st>>>(
-      state_ev, ELEM_STATE, (long long)field * 125, 0, ref, E, to_ref, 0);
+      state_ev, ELEM_STATE, (long long)field * 125, 0, ref, E, to_ref);
   return cudaGetLastError();
 }
 

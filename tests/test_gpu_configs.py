@@ -162,28 +162,36 @@ def test_c4_batch_events_match_oracle(native, oracle_mod):
             o.close()
 
 
-def test_c3_adjoint_kernels_match_oracle(native, oracle_mod):
+@pytest.mark.parametrize("lean", [False, True])
+def test_c3_adjoint_kernels_match_oracle(native, oracle_mod, lean):
     """64 x 64 x 32: forward run with records (samp_ad 10, 30 steps) and adjoint run with the
     ses3d_grad_Q kernels (30 steps), each from its own random state, with adjoint sources
-    at five receivers; records and all kernels against the oracle."""
+    at five receivers; records and all kernels against the oracle. Lean runs (displacement
+    gradients outside the PML from the displacement) start with zero displacement
+    gradients, the condition they need; full-state runs with random ones."""
     from ses3d_gb300.solver import Simulation
     nt, samp = 30, 10
     p = synth.make_problem("c3", nt=nt, seed=1234, adjoint_flag=1)
     p.setup.samp_ad = samp
     fwd = random_state(p, 5)
     adj = random_state(p, 6)
+    if lean:
+        fwd = {k: a for k, a in fwd.items() if k not in GRADS}
+        adj = {k: a for k, a in adj.items() if k not in GRADS}
     loc = p.events[0].receivers.loc[:5].copy()
     loc[:, 2] = np.float32(1000.0)
     stf = np.random.default_rng(7).standard_normal((5, 3, nt)).astype(np.float32) * np.float32(1e9)
     names = ("rho", "cp", "csh", "csv", "Q_mu", "alpha_mu", "Q_kappa")
     with Simulation.from_problem(p, adjoint_flag=1, grad_variant=1) as sim:
         load_gpu(sim, fwd)
+        sim.set_lean(lean)
         sim.run()
         g_records = [sim.record(r) for r in range(sim.record_count())]
         g_sv = sim.saving_vector()
         assert sim.set_adjoint_sources(0, loc, stf) == 5
         sim.begin_adjoint()
         load_gpu(sim, adj)
+        sim.set_lean(lean)
         sim.run()
         g_kernels = {k: sim.kernel(k) for k in names}
         g_v = sim.field("vz_global")
@@ -196,7 +204,7 @@ def test_c3_adjoint_kernels_match_oracle(native, oracle_mod):
         o.close()
         assert np.array_equal(sv, g_sv)
         assert len(recs) == len(g_records) == 4
-        tag = "c3 %s" % ("fp64" if fp64 else "fp32")
+        tag = "c3%s %s" % (" lean" if lean else "", "fp64" if fp64 else "fp32")
         if fp64:
             for r in range(len(recs)):
                 for f in range(9):
