@@ -472,7 +472,9 @@ int launch_iteration(ses3d_gpu *h, const Wave &w, int mode, float *rec, bool tim
   h->state_zero = false;
   p.state = w.state;
   p.v = w.v;
-  p.u = h->has_u ? w.v + (size_t)h->cfg.n_events * 3 * h->geo.G : nullptr;
+  // the displacement is integrated in lean runs, the only ones that read it (the stepping of
+  // a run with records is fixed for the run, so u covers every iteration since its start)
+  p.u = (h->has_u && h->c.lean) ? w.v + (size_t)h->cfg.n_events * 3 * h->geo.G : nullptr;
   p.d_it = w.d_it;
   p.rec = rec;
   p.src_elem = w.adjoint ? h->d_src_none : h->d_src_elem;
