@@ -291,14 +291,21 @@ class MisfitSetup:
         # per event: element state, velocity and displacement, element forces, FP64 kernels
         event = (36.0 * N + 6.0 * G + 3.0 * N) * 4 + 64.0 * N
         rec = 36.0 * N
-        ckpt = (36.0 * N + 6.0 * G) * 4
+        wave2 = (36.0 * N + 6.0 * G) * 4       # the recomputing wavefield
+        if self.lean:   # lean runs checkpoint 24 fields per element, all 36 in PML elements
+            p = int(c.pml)
+            ex, ey, ez = c.nx + 1, c.ny + 1, c.nz + 1
+            e_pml = E - max(0, ex - 2 * p) * max(0, ey - 2 * p) * max(0, ez - p)
+            ckpt = (24.0 * N + 12.0 * 125 * e_pml + 6.0 * G) * 4
+        else:
+            ckpt = wave2
         K = max(1, int(round(math.sqrt(nrec * ckpt / rec))))
-        one = event + ckpt + math.ceil(nrec / K) * ckpt + K * rec
+        one = event + wave2 + math.ceil(nrec / K) * ckpt + K * rec
         best = None
         for K1 in range(2, max(3, nrec + 1)):
             k2c = max(1, min(K1 - 1, int(round(math.sqrt(K1 * ckpt / rec)))))
             for K2 in range(max(1, k2c - 2), min(K1 - 1, k2c + 2) + 1):
-                mem = ckpt + math.ceil(nrec / K1) * ckpt + (math.ceil(K1 / K2) - 1) * ckpt + K2 * rec
+                mem = wave2 + math.ceil(nrec / K1) * ckpt + (math.ceil(K1 / K2) - 1) * ckpt + K2 * rec
                 if best is None or mem < best[0]:
                     best = (mem, K1, K2)
         return {"shared": shared, "keep": event + nrec * rec, "one_level": one, "K": K,

@@ -46,6 +46,8 @@ cudaError_t launch_gather_ref(const Consts &c, const float *v, float *out, cudaS
 cudaError_t prepare_element_kernels();
 cudaError_t prepare_adjoint_kernels();
 cudaError_t launch_sync_mirrors(const Consts &c, float *state, cudaStream_t st);
+cudaError_t launch_compact_state(const Consts &c, float *state, float *ck, const int *pml_el, long long npml, int to_ck,
+                                 cudaStream_t st);
 cudaError_t launch_wait_selftest(int *err, unsigned long long limit_ns, cudaStream_t st);
 cudaError_t launch_sum_events_d(const double *grad, int slot, int nev, long long N, double *out, cudaStream_t st);
 cudaError_t launch_state_field(float *state_ev, int field, float *ref, long long E, int to_ref, cudaStream_t st);
@@ -113,6 +115,8 @@ struct ses3d_gpu {
                             // hold the displacement [nev][3][G] after the velocity
   bool fwd_lean = false;    // the forward run with records stepped lean (its recomputes do too)
   bool du_set = false;      // displacement gradients were set since the wavefield was zeroed
+  int *d_pml_el = nullptr;  // PML elements in ascending order (compact checkpoints of lean runs)
+  long long n_pml_el = 0;
   int *d_aniso = nullptr;   // set by the model derivation when A, B or C is non-zero
   int *d_it = nullptr;
   int *d_err = nullptr;  // device error word (bounded waits)
@@ -508,16 +512,41 @@ size_t ckpt_floats(const ses3d_gpu *h) {
   return (size_t)h->cfg.n_events * (size_t)NSTATE * h->geo.N + v_floats(h);
 }
 
+// Element-state floats of a compact checkpoint (lean runs): 24 fields of every element and
+// the other 12 of the PML elements, all events.
+size_t compact_state_floats(const ses3d_gpu *h) {
+  return (size_t)h->cfg.n_events * 125 * (24 * (size_t)h->geo.E + 12 * (size_t)h->n_pml_el);
+}
+
+// Floats of one record checkpoint: compact when the forward run with records steps lean
+// (its recomputes read no other fields), else the full state.
+size_t rec_ckpt_floats(const ses3d_gpu *h) {
+  return h->fwd_lean ? compact_state_floats(h) + v_floats(h) : ckpt_floats(h);
+}
+
+// A wavefield (element state, velocity and displacement) into a checkpoint, or back.
+int wave_to_ckpt(ses3d_gpu *h, float *state, float *v, float *ck, bool compact, bool to_ck) {
+  const size_t ns = compact ? compact_state_floats(h) : (size_t)h->cfg.n_events * NSTATE * h->geo.N;
+  if (compact) {
+    CK(h, launch_compact_state(h->c, state, ck, h->d_pml_el, h->n_pml_el, to_ck ? 1 : 0, h->st));
+    ++h->launches;
+  } else if (to_ck) {
+    CK(h, cudaMemcpyAsync(ck, state, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  } else {
+    CK(h, cudaMemcpyAsync(state, ck, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  }
+  if (to_ck) CK(h, cudaMemcpyAsync(ck + ns, v, v_floats(h) * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  else CK(h, cudaMemcpyAsync(v, ck + ns, v_floats(h) * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  return SES3D_OK;
+}
+
 int save_checkpoint(ses3d_gpu *h, int completed_it) {
   Range range_("ses3d checkpoint");
-  const size_t ns = (size_t)h->cfg.n_events * NSTATE * h->geo.N;
   float *c = nullptr;
-  CK(h, dalloc(&c, ckpt_floats(h)));
+  CK(h, dalloc(&c, rec_ckpt_floats(h)));
   h->ckpts.push_back(c);
   h->ckpt_it.push_back(completed_it);
-  CK(h, cudaMemcpyAsync(c, h->d_state, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
-  CK(h, cudaMemcpyAsync(c + ns, h->d_v, v_floats(h) * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
-  return SES3D_OK;
+  return wave_to_ckpt(h, h->d_state, h->d_v, c, h->fwd_lean, true);
 }
 
 // Grows `views` to `count` buffers of `floats` each (rounded up to 256 bytes), carved from
@@ -557,14 +586,13 @@ int ensure_wave2(ses3d_gpu *h) {
   return SES3D_OK;
 }
 
-// Loads a full-state checkpoint (completed iterations it0) into the second wavefield.
-int load_wave2(ses3d_gpu *h, const float *ckpt, const int &it0) {
-  const size_t ns = (size_t)h->cfg.n_events * NSTATE * h->geo.N;
-  const size_t nv = v_floats(h);
+// Loads a checkpoint (completed iterations it0; compact: a lean run's) into the second
+// wavefield.
+int load_wave2(ses3d_gpu *h, const float *ckpt, const int &it0, bool compact = false) {
   int rc = ensure_wave2(h);
   if (rc) return rc;
-  CK(h, cudaMemcpyAsync(h->d_state2, ckpt, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
-  CK(h, cudaMemcpyAsync(h->d_v2, ckpt + ns, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  rc = wave_to_ckpt(h, h->d_state2, h->d_v2, const_cast<float *>(ckpt), compact, false);
+  if (rc) return rc;
   CK(h, cudaMemcpyAsync(h->d_it2, &it0, sizeof(int), cudaMemcpyHostToDevice, h->st));
   return SES3D_OK;
 }
@@ -608,7 +636,7 @@ int recompute_records(ses3d_gpu *h, int it0, int rA, int rB) {
 // into segbuf by a forward run from checkpoint s on the second wavefield.
 int recompute_segment(ses3d_gpu *h, int s) {
   Range range_("ses3d recompute segment");
-  int rc = load_wave2(h, h->ckpts[s], h->ckpt_it[s]);
+  int rc = load_wave2(h, h->ckpts[s], h->ckpt_it[s], h->fwd_lean);
   if (rc) return rc;
   const int r0 = s * h->ckpt_K;
   const int r1 = std::min((int)h->store_steps.size(), r0 + h->ckpt_K);
@@ -627,15 +655,13 @@ int recompute_level2(ses3d_gpu *h, int s) {
   const int r0 = s * h->ckpt_K;
   const int r1 = std::min((int)h->store_steps.size(), r0 + h->ckpt_K);
   const int nsub = (r1 - r0 + h->ckpt_K2 - 1) / h->ckpt_K2;
-  const size_t ns = (size_t)h->cfg.n_events * NSTATE * h->geo.N;
-  const size_t nv = v_floats(h);
   while ((int)h->ckpt2.size() < nsub - 1) {
     float *c = nullptr;
-    CK(h, dalloc(&c, ckpt_floats(h)));
+    CK(h, dalloc(&c, rec_ckpt_floats(h)));
     h->ckpt2.push_back(c);
   }
   h->ckpt2_it.assign(std::max(0, nsub - 1), 0);
-  int rc = load_wave2(h, h->ckpts[s], h->ckpt_it[s]);
+  int rc = load_wave2(h, h->ckpts[s], h->ckpt_it[s], h->fwd_lean);
   if (rc) return rc;
   Wave w{h->d_state2, h->d_v2, h->d_it2, false, false};
   int it = h->ckpt_it[s];
@@ -645,8 +671,8 @@ int recompute_level2(ses3d_gpu *h, int s) {
       rc = launch_iteration(h, w, 0, nullptr);
       if (rc) return rc;
     }
-    CK(h, cudaMemcpyAsync(h->ckpt2[j - 1], h->d_state2, ns * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
-    CK(h, cudaMemcpyAsync(h->ckpt2[j - 1] + ns, h->d_v2, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+    rc = wave_to_ckpt(h, h->d_state2, h->d_v2, h->ckpt2[j - 1], h->fwd_lean, true);
+    if (rc) return rc;
     h->ckpt2_it[j - 1] = target;
   }
   h->seg_loaded = s;
@@ -678,7 +704,7 @@ int checkpointed_record(ses3d_gpu *h, int r, float **out) {
     const int rB = std::min({(int)h->store_steps.size(), r0 + h->ckpt_K, rA + h->ckpt_K2});
     const float *src = j == 0 ? h->ckpts[s] : h->ckpt2[j - 1];
     const int it0 = j == 0 ? h->ckpt_it[s] : h->ckpt2_it[j - 1];
-    int rc = load_wave2(h, src, it0);
+    int rc = load_wave2(h, src, it0, h->fwd_lean);
     if (!rc) rc = recompute_records(h, it0, rA, rB);
     if (rc) return rc;
     h->sub_loaded = j;
@@ -843,6 +869,19 @@ int ses3d_gpu_create(const ses3d_config *cfg, ses3d_gpu **out) {
   chk(dalloc(&h->d_mat, (size_t)ELEM_MAT * g.E));
   chk(dalloc(&h->d_err, 1));
   chk(dalloc(&h->d_aniso, 1));
+  {  // PML elements (pml elements on the x and y sides and at the bottom), ascending
+    std::vector<int> pel;
+    for (int k = 0; k < g.ez; ++k)
+      for (int j = 0; j < g.ey; ++j)
+        for (int i = 0; i < g.ex; ++i)
+          if (i < cfg->pml || i >= g.ex - cfg->pml || j < cfg->pml || j >= g.ey - cfg->pml || k >= g.ez - cfg->pml)
+            pel.push_back(i + g.ex * (j + g.ey * k));
+    h->n_pml_el = (long long)pel.size();
+    if (!pel.empty()) {
+      chk(dalloc(&h->d_pml_el, pel.size()));
+      if (e == cudaSuccess) chk(cudaMemcpy(h->d_pml_el, pel.data(), pel.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
+  }
   chk(dalloc(&h->d_gmat, (size_t)NGMAT * g.N));
   chk(dalloc(&h->d_state, nev * NSTATE * g.N));
   h->has_u = cfg->adjoint_flag >= 1;
@@ -911,7 +950,7 @@ int ses3d_gpu_destroy(ses3d_gpu *h) {
   void *ptrs[] = {h->d_ktab, h->d_tab, h->d_MM, h->d_mat, h->d_gmat, h->d_state, h->d_v, h->d_f, h->d_it,
                   h->d_src_elem, h->d_src_delta, h->d_src_mom, h->d_stf, h->d_src_none, h->d_rec_elem,
                   h->d_rec_ev, h->d_rec_w, h->d_seis, h->d_grad, h->d_scratch_u, h->d_state2, h->d_v2, h->d_it2, h->d_err,
-                  h->d_aniso};
+                  h->d_aniso, h->d_pml_el};
   for (void *p : ptrs) dfree(p);
   free_forces(h->fset[0]);
   free_forces(h->fset[1]);
@@ -1633,9 +1672,9 @@ int64_t ses3d_gpu_memory_bytes(const ses3d_gpu *h) {
   size_t bytes = f * sizeof(float);
   if (h->d_grad) bytes += nev * NGRAD * N * sizeof(double);
   bytes += std::max(h->records.size(), h->record_slots.size()) * nev * NREC * N * sizeof(float);
-  bytes += h->ckpts.size() * ckpt_floats(h) * sizeof(float);
+  bytes += h->ckpts.size() * rec_ckpt_floats(h) * sizeof(float);
   bytes += h->segbuf.size() * nev * NREC * N * sizeof(float);
-  bytes += h->ckpt2.size() * ckpt_floats(h) * sizeof(float);
+  bytes += h->ckpt2.size() * rec_ckpt_floats(h) * sizeof(float);
   bytes += h->ex_block_floats * sizeof(float);
   if (h->d_astate) bytes += nev * (((size_t)NSTATE * N + 6 * G + 3 * N) * sizeof(float) + ((size_t)NMAT * N + G) * sizeof(double));
   if (h->d_state2) bytes += (nev * (size_t)NSTATE * N + v_floats(h)) * sizeof(float);

@@ -1006,6 +1006,31 @@ __global__ void k_blocked_ref(float *__restrict__ blocked, long long stride, lon
   }
 }
 
+// Compact state of a lean run (checkpoints): fields 0-5 and 18-35 of every element, 24 x 125
+// floats per element, then fields 6-17 (mirror stresses, displacement gradients) of the PML
+// elements in the order of pml_el; lean iterations read no others. to_ck: state -> ck, else
+// ck -> state (the fields left out keep what they held).
+__global__ void k_compact_state(const Consts c, float *__restrict__ state, float *__restrict__ ck,
+                                const int *__restrict__ pml_el, long long npml, int to_ck) {
+  const long long partA = (long long)c.nev * c.E * 24 * 125, partB = (long long)c.nev * npml * 12 * 125;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < partA + partB;
+       q += (long long)gridDim.x * blockDim.x) {
+    long long s;
+    if (q < partA) {
+      const long long r = q / 125, n = q - r * 125;
+      const long long el = r / 24, fi = r - el * 24;
+      s = (el * NSTATE + (fi < 6 ? fi : fi + 12)) * 125 + n;
+    } else {
+      const long long q2 = q - partA, r = q2 / 125, n = q2 - r * 125;
+      const long long r2 = r / 12, fi = r - r2 * 12;
+      const long long ev = r2 / npml, pe = r2 - ev * npml;
+      s = ((ev * c.E + pml_el[pe]) * NSTATE + 6 + fi) * 125 + n;
+    }
+    if (to_ck) ck[q] = state[s];
+    else state[s] = ck[q];
+  }
+}
+
 // Mirror stresses of the elements outside the PML from their partners (syx = sxy,
 // szx = sxz, szy = syz there), after lean iterations that left them out.
 __global__ void k_sync_mirrors(const Consts c, float *__restrict__ state) {
@@ -1323,6 +1348,15 @@ cudaError_t launch_mass(const Consts &c, const float *rhoinv, const float *z, co
 cudaError_t launch_state_field(float *state_ev, int field, float *ref, long long E, int to_ref, cudaStream_t st) {
   k_blocked_ref<<<dim3((unsigned)((E + 31) / 32), 4, 1), dim3(32, 8), 0, st>>>(
       state_ev, ELEM_STATE, (long long)field * 125, 0, ref, E, to_ref);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compact_state(const Consts &c, float *state, float *ck, const int *pml_el, long long npml, int to_ck,
+                                 cudaStream_t st) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  k_compact_state<<<(unsigned)((sms > 0 ? sms : 1) * 8), 256, 0, st>>>(c, state, ck, pml_el, npml, to_ck);
   return cudaGetLastError();
 }
 
