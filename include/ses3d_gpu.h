@@ -210,8 +210,10 @@ int ses3d_gpu_put_record(ses3d_gpu *h, int event, int record, const float *in);
  * every event) before every K-th stored iteration instead of the records, and the flag-2
  * run recomputes the records of one segment at a time from its checkpoint on a second
  * wavefield (one extra forward pass in total). K = 0 (default) keeps every record in
- * device memory. Memory with K > 0: ceil(nrec / K) checkpoints of (36 N + 3 G) floats,
- * K records of 9 N floats and one extra wavefield, per event. Call before the flag-1
+ * device memory. Memory with K > 0: ceil(nrec / K) checkpoints, K records of 9 N floats
+ * and one extra wavefield, per event. A checkpoint holds the element state (36 N floats,
+ * or with lean stepping 24 N + 1500 E_pml: outside the PML the fields lean iterations do
+ * not read are left out), the velocity and the displacement (6 G). Call before the flag-1
  * run starts. Replaces the disk store/restore of SOURCE/ses3d_output.f90:5-267. */
 int ses3d_gpu_set_checkpointing(ses3d_gpu *h, int records_per_segment);
 
@@ -220,8 +222,9 @@ int ses3d_gpu_set_checkpointing(ses3d_gpu *h, int records_per_segment);
  * K2-th of its records, and then each sub-segment of K2 records from those as the adjoint
  * run reaches it (two extra forward passes in total). Memory per event: ceil(nrec / K)
  * + ceil(K / K2) - 1 checkpoints, K2 records and one extra wavefield -- for 96 x 96 x 40,
- * nt = 4000, samp_ad = 10 (401 records of 1.66 GB, checkpoints of 6.9 GB) K = 81, K2 = 9
- * need 110 GB against 155 GB with one level. K2 = 0 is ses3d_gpu_set_checkpointing(h, K).
+ * nt = 4000, samp_ad = 10 (401 records of 1.66 GB, full-state checkpoints of 7.2 GB)
+ * K = 81, K2 = 21 need about 114 GB against 163 GB with one level (lean runs' 5.4-GB
+ * checkpoints: one level, K = 36, about 146 GB). K2 = 0 is ses3d_gpu_set_checkpointing(h, K).
  * Extends the disk store/restore of SOURCE/ses3d_output.f90:5-267 (no counterpart). */
 int ses3d_gpu_set_checkpoint_levels(ses3d_gpu *h, int records_per_segment, int records_per_subsegment);
 
