@@ -570,6 +570,24 @@ __device__ __forceinline__ void gather_v_async(const Consts &c, const Ptrs &p, l
   asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
+// L2 prefetch of what a correlation item's epilogue reads with plain loads (the forward
+// record, the adjoint-model fields and the FP64 kernel accumulators at the item's points),
+// issued one item ahead by the threads that will read them.
+template <bool DISS>
+__device__ __forceinline__ void prefetch_corr(const Consts &c, const Ptrs &p, long long item, int nn) {
+  const int ev = (int)(item % c.nev);
+  const size_t N = (size_t)c.N, m0 = (size_t)(item / c.nev) * 125 + nn;
+  const float *R = p.rec + (size_t)ev * NREC * N + m0;
+#pragma unroll
+  for (int f = 0; f < NREC; ++f) prefetch_l2(R + f * N);
+  prefetch_l2(p.gmat + G_RHO * N + m0);
+  prefetch_l2(p.gmat + G_CP * N + m0);
+  prefetch_l2(p.gmat + G_CS * N + m0);
+  const double *GR = p.grad + (size_t)ev * NGRAD * N + m0;
+  const int nk = (DISS && p.grad_q) ? 8 : 4;
+  for (int q = 0; q < nk; ++q) prefetch_l2(GR + q * N);
+}
+
 // MINB: resident CTAs per SM requested from ptxas (register cap); REFILL: when the next
 // item's bulk copy is issued (0: the measured rule below, 1: the other point). PACK: also
 // write the fields of each item's starting state that the exact adjoint's transposed step
@@ -676,6 +694,8 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
     if (TMA_VBUF == 2 && item + stride < total)
       gather_v_async<TABLES>(c, p, item + stride, s_vb + 3 * ((t + 1) % 2), s_lt + LT_FLOATS * ((t + 1) % 2), n, in,
                              jn, kn);
+    if constexpr (corr_mode(MODE))
+      if (on && p.rec && item + stride < total) prefetch_corr<DISS>(c, p, item + stride, nn);
     const long long refill = item + TMA_STAGES * stride;
     auto issue_refill = [&]() {
       if (n == 0 && refill < total) {
