@@ -48,7 +48,16 @@ struct ElemCtx {
   float *S;  // this node's state in global memory: field f at S[f * 125]
   float vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC;
   const float *lt;  // this element's 1-D table entries in shared memory (LT_*), or null
+  // Correlation operands staged in shared memory by cp.async (persistent kernel), or null:
+  // [CS_FLOATS][TPE] floats (record, adjoint model), then [NGRAD][TPE] doubles (kernels).
+  float *cstage;
+  bool cstage_more;       // a later cp.async group (the next item's velocity) is in flight
+  long long cstage_next;  // item whose operands to stage once these are consumed, or -1
 };
+
+// Correlation operands per point: the NREC record fields, then rho, cp, cs.
+constexpr int CS_FLOATS = 12;
+constexpr size_t CS_BYTES = CS_FLOATS * 128 * sizeof(float) + 8 * 128 * sizeof(double);
 
 // Per-element copy of the 1-D tables (five entries per axis) and the event's source
 // element, prefetched into shared memory by the persistent element kernel.
@@ -72,6 +81,29 @@ __host__ __device__ constexpr bool corr_mode(int m) { return m == 2 || m == 5; }
 struct NoHook {
   __device__ void operator()() const {}
 };
+
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+// Stages one point's correlation operands of `item` (thread nn of its element) into cs, as
+// one cp.async group: the forward record, the adjoint-model fields, the FP64 kernels.
+template <bool DISS>
+__device__ __forceinline__ void stage_corr(const Consts &c, const Ptrs &p, long long item, int nn, float *cs) {
+  const int ev = (int)(item % c.nev);
+  const size_t N = (size_t)c.N, m0 = (size_t)(item / c.nev) * 125 + nn;
+  const float *R = p.rec + (size_t)ev * NREC * N + m0;
+#pragma unroll
+  for (int f = 0; f < NREC; ++f) cp_async4(cs + f * TPE + nn, R + f * N);
+  cp_async4(cs + 9 * TPE + nn, p.gmat + G_RHO * N + m0);
+  cp_async4(cs + 10 * TPE + nn, p.gmat + G_CP * N + m0);
+  cp_async4(cs + 11 * TPE + nn, p.gmat + G_CS * N + m0);
+  double *cd = reinterpret_cast<double *>(cs + CS_FLOATS * TPE) + nn;
+  const double *GR = p.grad + (size_t)ev * NGRAD * N + m0;
+  const int nk = (DISS && p.grad_q) ? 8 : 4;
+  for (int q = 0; q < nk; ++q) cp_async8(cd + q * TPE, GR + q * N);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
 
 // after_barrier() runs on every thread right after the barrier between the stress and
 // divergence phases (the persistent kernel issues its next bulk copies there).
@@ -309,24 +341,44 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
       R[R_EXY * N] = (dxuy + dyux) * 0.5f; R[R_EXZ * N] = (dxuz + dzux) * 0.5f; R[R_EYZ * N] = (dyuz + dzuy) * 0.5f;
     }
     if (corr_mode(MODE) && p.rec) {  // kernel correlation (ses3d_grad.f90:53-83, ses3d_grad_Q.f90:111-143)
-      const float *R = p.rec + (size_t)ev * NREC * N + m0;
-      const float vxf = R[R_VX * N], vyf = R[R_VY * N], vzf = R[R_VZ * N];
-      const float exxf = R[R_EXX * N], eyyf = R[R_EYY * N], ezzf = R[R_EZZ * N];
-      const float exyf = R[R_EXY * N], exzf = R[R_EXZ * N], eyzf = R[R_EYZ * N];
+      // operands from the shared-memory stage when the persistent kernel staged them
+      const float *cf = x.cstage;
+      size_t fs = TPE;
+      if (cf) {
+        if (x.cstage_more) asm volatile("cp.async.wait_group 1;" ::: "memory");
+        else asm volatile("cp.async.wait_group 0;" ::: "memory");
+        cf += n;
+      } else {
+        cf = p.rec + (size_t)ev * NREC * N + m0;
+        fs = N;
+      }
+      const float *R = cf;
+      const float vxf = R[R_VX * fs], vyf = R[R_VY * fs], vzf = R[R_VZ * fs];
+      const float exxf = R[R_EXX * fs], eyyf = R[R_EYY * fs], ezzf = R[R_EZZ * fs];
+      const float exyf = R[R_EXY * fs], exzf = R[R_EXZ * fs], eyzf = R[R_EYZ * fs];
       const float exx_ad = dxux, eyy_ad = dyuy, ezz_ad = dzuz;
       const float exy_ad = 0.5f * (dxuy + dyux), exz_ad = 0.5f * (dxuz + dzux), eyz_ad = 0.5f * (dyuz + dzuy);
       const float tr_ad = exx_ad + eyy_ad + ezz_ad, tr_fw = exxf + eyyf + ezzf;
       const float edde = exx_ad * exxf + eyy_ad * eyyf + ezz_ad * ezzf + 2.f * exy_ad * exyf +
                          2.f * exz_ad * exzf + 2.f * eyz_ad * eyzf;
-      const float *GM = p.gmat + m0;
-      const float rho = GM[G_RHO * N], cp = GM[G_CP * N], cs = GM[G_CS * N];
+      float rho, cp, cs;
+      if (x.cstage) {
+        rho = cf[9 * TPE]; cp = cf[10 * TPE]; cs = cf[11 * TPE];
+      } else {
+        const float *GM = p.gmat + m0;
+        rho = GM[G_RHO * N]; cp = GM[G_CP * N]; cs = GM[G_CS * N];
+      }
+      const double *G0 = x.cstage ? reinterpret_cast<const double *>(x.cstage + CS_FLOATS * TPE) + n
+                                  : p.grad + (size_t)ev * NGRAD * N + m0;
+      const size_t gs = x.cstage ? (size_t)TPE : N;
       const double sj = c.s_jac;
       double *GR = p.grad + (size_t)ev * NGRAD * N + m0;
-      GR[0 * N] += sj * (double)((vxf * vx + vyf * vy + vzf * vz) +
-                                 ((cp * cp - 2.f * cs * cs) * tr_fw * tr_ad + 2.f * cs * cs * edde));
-      GR[1 * N] += sj * (double)(2.f * rho * cp * tr_fw * tr_ad);
-      GR[2 * N] += sj * (double)(4.f * rho * cs * (edde - tr_ad * tr_fw - 2.f * exzf * exz_ad - 2.f * eyzf * eyz_ad));
-      GR[3 * N] += sj * (double)(8.f * rho * cs * (exzf * exz_ad + eyzf * eyz_ad));
+      GR[0 * N] = G0[0 * gs] + sj * (double)((vxf * vx + vyf * vy + vzf * vz) +
+                                            ((cp * cp - 2.f * cs * cs) * tr_fw * tr_ad + 2.f * cs * cs * edde));
+      GR[1 * N] = G0[1 * gs] + sj * (double)(2.f * rho * cp * tr_fw * tr_ad);
+      GR[2 * N] = G0[2 * gs] + sj * (double)(4.f * rho * cs * (edde - tr_ad * tr_fw - 2.f * exzf * exz_ad -
+                                                               2.f * eyzf * eyz_ad));
+      GR[3 * N] = G0[3 * gs] + sj * (double)(8.f * rho * cs * (exzf * exz_ad + eyzf * eyz_ad));
       if (DISS && p.grad_q) {
         // The three mechanisms' terms are summed in FP32 and the sum accumulated in FP64:
         // one conversion and one FMA per kernel (FP64 issue is scarce on this part).
@@ -345,11 +397,13 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
           gk += Mk * c.tau_p[m];
           gak += Mk * c.q_alpha_w[m];
         }
-        GR[4 * N] += sj * (double)gq;
-        GR[5 * N] += sj * (double)ga;
-        GR[6 * N] += sj * (double)gk;
-        GR[7 * N] += sj * (double)gak;
+        GR[4 * N] = G0[4 * gs] + sj * (double)gq;
+        GR[5 * N] = G0[5 * gs] + sj * (double)ga;
+        GR[6 * N] = G0[6 * gs] + sj * (double)gk;
+        GR[7 * N] = G0[7 * gs] + sj * (double)gak;
       }
+      // this point's operands are in registers and used: stage the next item's
+      if (x.cstage && x.cstage_next >= 0) stage_corr<DISS>(c, p, x.cstage_next, nn, x.cstage);
     }
   }
   __syncthreads();
@@ -463,7 +517,8 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
   }
   s_v[sub][0][n] = vx; s_v[sub][1][n] = vy; s_v[sub][2][n] = vz;
   __syncthreads();
-  ElemCtx x{act, full, n, nn, in, jn, kn, ii, j, k, ev, e, N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC, nullptr};
+  ElemCtx x{act, full, n, nn, in, jn, kn, ii, j, k, ev, e, N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC, nullptr,
+            nullptr, false, -1};
   element_compute<DISS, MODE>(c, p, tab, s_v[sub], s_p[sub], x, sv);
 }
 
@@ -502,6 +557,10 @@ constexpr size_t TMA_LT_OFF =
     TMA_STAGES * sizeof(ElemStage) + (9 + 3 * TMA_VBUF) * TPE * sizeof(float) + ((sizeof(KTab) + 15) / 16) * 16;
 constexpr size_t TMA_BAR_OFF = TMA_LT_OFF + TMA_VBUF * LT_FLOATS * sizeof(float);
 constexpr size_t TMA_SMEM = TMA_BAR_OFF + TMA_STAGES * sizeof(unsigned long long);
+// Correlation iterations also stage their epilogue operands (CS_BYTES) behind the barriers.
+constexpr size_t TMA_CS_OFF = (TMA_SMEM + 15) / 16 * 16;
+__host__ __device__ constexpr bool tma_cstage(int mode) { return corr_mode(mode) && TMA_VBUF == 2; }
+__host__ __device__ constexpr size_t tma_smem(int mode) { return tma_cstage(mode) ? TMA_CS_OFF + CS_BYTES : TMA_SMEM; }
 
 // Copies of one item into a stage. Byte ranges (element block of 18,000 B, fields of 500 B):
 // all 36 fields; elastic: fields 0-17 (9,008 B, the last 8 B inside field 18); lean outside
@@ -622,6 +681,12 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
   const int in = nn % 5, jn = (nn / 5) % 5, kn = nn / 25;
   constexpr bool TABLES = lean_mode(MODE);
   if (TMA_VBUF == 2 && first < total) gather_v_async<TABLES>(c, p, first, s_vb, s_lt, n, in, jn, kn);
+  // correlation operands: staged one item ahead, each thread its own point (cp.async groups
+  // in the order velocity(t), operands(t), velocity(t + 1), operands(t + 1), ...)
+  float *cstage = nullptr;
+  if constexpr (tma_cstage(MODE))
+    if (p.rec) cstage = reinterpret_cast<float *>(smem + TMA_CS_OFF);
+  if (cstage && on && first < total) stage_corr<DISS>(c, p, first, nn, cstage);
   for (int t = 0;; ++t) {
     const long long item = first + (long long)t * stride;
     if (item >= total) break;
@@ -635,7 +700,8 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
     const bool full = !lean_mode(MODE) || in_pml_element(c, i, j, k);
     float vx = 0.f, vy = 0.f, vz = 0.f;
     if (TMA_VBUF == 2) {  // this item's velocity was gathered one item ahead
-      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      if (cstage) asm volatile("cp.async.wait_group 1;" ::: "memory");  // operands(t) may stay in flight
+      else asm volatile("cp.async.wait_group 0;" ::: "memory");
       if (on) { vx = s_v[0][n]; vy = s_v[1][n]; vz = s_v[2][n]; }
     } else if (on) {
       // gather v_global -> element-local v (ses3d_evolution.f90:27-51), issued before the wait
@@ -682,6 +748,7 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
     }
     if (TMA_VBUF == 1) { s_v[0][n] = vx; s_v[1][n] = vy; s_v[2][n] = vz; }
     if (__syncthreads_or(!ok)) {  // a copy never arrived: drain the stages, then leave
+      asm volatile("cp.async.wait_all;" ::: "memory");
       if (n == 0) {
         mbar_wait_bounded(&bar[s], parity, p.err);
         if constexpr (TMA_STAGES == 2)
@@ -712,7 +779,9 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
     const size_t m0 = (size_t)e * 125 + nn;
     float *S = p.state + ((size_t)ev * c.E + e) * ELEM_STATE + nn;
     const float *lt = (TMA_VBUF == 2 && TABLES) ? s_lt + LT_FLOATS * (t % 2) : nullptr;
-    ElemCtx x{on, full, n, nn, in, jn, kn, i, j, k, ev, e, (size_t)c.N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC, lt};
+    const bool more = item + stride < total;
+    ElemCtx x{on,  full, n,  nn, in, jn, kn, i, j, k, ev, e, (size_t)c.N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2,
+              cC,  lt,   cstage, TMA_VBUF == 2 && more, more ? item + stride : -1};
     if (LATE_REFILL) element_compute<DISS, MODE>(c, p, *tab, s_v, s_p, x, sv, issue_refill);
     else element_compute<DISS, MODE>(c, p, *tab, s_v, s_p, x, sv);
   }
@@ -1166,12 +1235,12 @@ static int &tma_grid_cap() {
 template <bool DISS, int MODE, int S, bool PACK = false>
 static cudaError_t prepare_tma() {
   auto kern = k_element_tma<DISS, MODE, TmaShape<S>::minb, TmaShape<S>::refill, PACK>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TMA_SMEM);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tma_smem(MODE));
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TPE, TMA_SMEM);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TPE, tma_smem(MODE));
   if (e != cudaSuccess) return e;
   tma_grid_cap<DISS, MODE, S, PACK>() = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
   return cudaSuccess;
@@ -1212,7 +1281,7 @@ static cudaError_t launch_tma(const Consts &c, const Ptrs &p, cudaStream_t st) {
   if (grid_cap <= 0) return cudaErrorInitializationError;
   const long long total = c.E * (long long)c.nev;
   const unsigned blocks = (unsigned)(total < grid_cap ? total : grid_cap);
-  k_element_tma<DISS, MODE, TmaShape<S>::minb, TmaShape<S>::refill, PACK><<<blocks, TPE, TMA_SMEM, st>>>(c, p);
+  k_element_tma<DISS, MODE, TmaShape<S>::minb, TmaShape<S>::refill, PACK><<<blocks, TPE, tma_smem(MODE), st>>>(c, p);
   return cudaGetLastError();
 }
 
