@@ -105,6 +105,65 @@ def test_record_and_correlation_kernels_bit_identical(native, is_diss):
         assert np.abs(a).max() > 0 and np.array_equal(a, b), k
 
 
+def random_velocities(sim, nev, rng):
+    for ev in range(nev):
+        for k in ("vx_global", "vy_global", "vz_global"):
+            n = sim.field(k, ev).size
+            sim.set_field(k, (1e-3 * rng.standard_normal(n)).astype(np.float32), ev)
+
+
+def correlation_run(p, epb, nt, lean, seed):
+    """Forward with records from random initial velocities, then the adjoint run from random
+    velocities with random adjoint sources at two receivers of every event, so that every
+    element holds forward and adjoint fields and every correlation item contributes."""
+    from ses3d_gb300.solver import Simulation
+    rng = np.random.default_rng(seed)
+    nev = len(p.events)
+    names = ("rho", "cp", "csh", "csv", "Q_mu", "alpha_mu", "Q_kappa")
+    sim = Simulation.from_problem(p, adjoint_flag=1, grad_variant=1)
+    try:
+        sim.set_block_elements(epb)
+        sim.set_lean(lean)
+        random_velocities(sim, nev, rng)
+        sim.run()
+        records = [sim.record(r, ev) for ev in range(nev) for r in range(sim.record_count())]
+        for ev in range(nev):
+            stf = (1e10 * rng.standard_normal((2, 3, nt))).astype(np.float32)
+            sim.set_adjoint_sources(ev, p.events[ev].receivers.loc[:2].copy(), stf)
+        sim.begin_adjoint()
+        random_velocities(sim, nev, rng)
+        sim.run()
+        return records, [sim.kernel(k, ev) for ev in range(nev) for k in names]
+    finally:
+        sim.close()
+
+
+@pytest.mark.parametrize("n_events", [1, 2])
+def test_correlation_with_several_items_per_cta(native, n_events):
+    """On a 20 x 20 x 10 mesh (4,000 elements per event) each CTA of the persistent element
+    kernel steps several items, staging the next item's record, adjoint model and FP64
+    kernels while it works on the current one. Records and kernels equal the register-staged
+    kernel's bit for bit; lean runs (displacement gradients from the displacement outside the
+    PML) follow within FP32 rounding."""
+    nt = 40
+    p = synth.make_problem("small", nt=nt, seed=89, adjoint_flag=1, n_el=(20, 20, 10), n_events=n_events)
+    p.setup.samp_ad = 4
+    rec_r, ker_r = correlation_run(p, 2, nt, False, 5)
+    rec_p, ker_p = correlation_run(p, 1, nt, False, 5)
+    rec_l, ker_l = correlation_run(p, 1, nt, True, 5)
+    assert len(rec_r) == n_events * (1 + nt // 4)
+    for a, b in zip(rec_r, rec_p):
+        assert np.array_equal(a, b)
+    for k, (a, b) in enumerate(zip(ker_r, ker_p)):
+        assert np.abs(a).max() > 0 and np.array_equal(a, b), k
+    rel = lambda a, b: float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+    for r, (a, b) in enumerate(zip(rec_l, rec_r)):
+        if np.abs(b).max() > 0:
+            assert rel(a, b) <= 1e-4, (r, rel(a, b))
+    for k, (a, b) in enumerate(zip(ker_l, ker_r)):
+        assert rel(a, b) <= 1e-3, (k, rel(a, b))
+
+
 def test_isotropy_follows_the_model_and_drops_the_graph(native):
     """The model's A, B, C decide whether the element kernels read three or six material
     fields: an isotropic model reports 1, a model with non-zero A, B, C set later in the run
