@@ -81,6 +81,19 @@ def test_dot_product_several_iterations(native, K, K2):
     assert abs(lhs - rhs) <= 1e-5 * abs(lhs)
 
 
+def test_dot_product_several_items_per_cta(native):
+    """The 20 x 20 x 10 mesh (4,000 elements): each CTA of the persistent forward and
+    transposed element kernels steps several elements, so the copies of the next item are in
+    flight while the current one is computed. Five iterations, checkpoints every 3."""
+    p = synth.make_problem("small", nt=5, seed=65, n_el=(20, 20, 10))
+    p.events[0].stf[:] = 0.0
+    x = independent_state(p, 7, 1)
+    y = independent_state(p, 8, 1)
+    lhs, rhs, _ = forward_then_backward(p, x, y, 5, 3, 1)
+    print("dot 20x20x10: %.9e %.9e rel %.2e" % (lhs, rhs, abs(lhs - rhs) / abs(lhs)))
+    assert abs(lhs - rhs) <= 1e-5 * abs(lhs)
+
+
 def one_iteration_misfit(p, x, y, names, model):
     from ses3d_gb300.solver import Simulation
     q = synth.Problem(p.setup, p.box, p.tau, p.D, model, p.events, pml=p.pml)
