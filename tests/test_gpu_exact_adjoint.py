@@ -239,16 +239,17 @@ def test_exact_misfit_gradient_matches_finite_differences(c3_misfit):
         assert err <= 1e-3, (nm, fd, ge)
 
 
-@pytest.mark.parametrize("K,K2", [(7, 0), (7, 3)])
-def test_lean_forward_gives_the_same_gradient(native, K, K2):
+@pytest.mark.parametrize("K,K2,n_el", [(7, 0, None), (7, 3, None), (7, 3, (20, 20, 10))])
+def test_lean_forward_gives_the_same_gradient(native, K, K2, n_el):
     """A run from rest stepped lean (elements outside the PML keep neither displacement
     gradients nor mirror stresses) gives the exact gradient and the adjoint of the initial
-    state of the full-state run bit for bit, with one and two checkpoint levels; the
-    choice cannot change once the forward run has started."""
+    state of the full-state run bit for bit, with one and two checkpoint levels (and on a
+    20 x 20 x 10 mesh, several elements per CTA of the persistent kernels); the choice
+    cannot change once the forward run has started."""
     from ses3d_gb300 import _lib
     from ses3d_gb300.solver import Simulation
     nt = 30
-    p = synth.make_problem("small", nt=nt, seed=64)
+    p = synth.make_problem("small", nt=nt, seed=64, n_el=n_el)
     out = []
     for lean in (False, True):
         with Simulation.from_problem(p) as sim:
