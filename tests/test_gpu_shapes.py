@@ -22,9 +22,13 @@ def run(p, steps, lean, shape, node_block, graph=10):
 
 
 @pytest.mark.parametrize("lean", [False, True])
-def test_all_shapes_bit_identical(native, lean):
+@pytest.mark.parametrize("n_el", [None, (20, 20, 10)])
+def test_all_shapes_bit_identical(native, lean, n_el):
+    """Every element shape and node block size gives the same bits, on the 10 x 9 x 6 mesh
+    (at most one element per CTA of the persistent kernel) and on 20 x 20 x 10 (several, so
+    that every shape's copy pipeline runs ahead of its compute)."""
     from ses3d_gb300 import _lib
-    p = synth.make_problem("small", nt=30, seed=81)
+    p = synth.make_problem("small", nt=30, seed=81, n_el=n_el)
     ref = run(p, 30, lean, 0, 256)
     assert np.abs(ref[0]).max() > 0
     n = int(_lib.load().ses3d_gpu_kernel_shape_count())
