@@ -89,6 +89,34 @@ def test_external_step_matches_step_two_calls(native):
                 assert np.array_equal(sbs[c], sa[c]), (call, c)
 
 
+def test_external_step_several_items_per_cta(native):
+    """A 20 x 20 x 10 mesh (several elements per CTA of the persistent element kernel) from
+    the same random initial velocity in both handles: two calls of three steps equal
+    ses3d_gpu_step bit for bit."""
+    import torch
+    from ses3d_gb300 import _lib
+    from ses3d_gb300.solver import Simulation
+    lib = _lib.load()
+    p = synth.make_problem("tiny", nt=12, seed=48, n_el=(20, 20, 10))
+    rng = np.random.default_rng(3)
+    with Simulation.from_problem(p) as a, Simulation.from_problem(p) as b:
+        vel = [(1e-3 * rng.standard_normal(a.G)).astype(np.float32) for _ in range(3)]
+        for name, x in zip(("vx_global", "vy_global", "vz_global"), vel):
+            a.set_field(name, x)
+        state = torch.zeros(36 * a.N, dtype=torch.float32, device="cuda")
+        v = torch.from_numpy(np.concatenate(vel)).to("cuda")
+        torch.cuda.synchronize()
+        for call in range(2):
+            a.step(3)
+            external(lib, b, state, v, 3)
+            torch.cuda.synchronize()
+            check_same(a, state, v, 1, STRESSES, extra=("dxux", "dzuy"))
+            sa, sbs = a.seismograms(0), b.seismograms(0)
+            for c in range(3):
+                assert np.abs(sa[c]).max() > 0
+                assert np.array_equal(sbs[c], sa[c]), (call, c)
+
+
 def test_external_step_two_events_lean_then_full(native):
     """Two events on a mesh with elements outside the PML: a lean call, then a call with
     lean stepping off (the mirror stresses of the caller's buffer are brought up to date
