@@ -53,6 +53,9 @@ struct ElemCtx {
   float *cstage;
   bool cstage_more;       // a later cp.async group (the next item's velocity) is in flight
   long long cstage_next;  // item whose operands to stage once these are consumed, or -1
+  // Displacement at this item's nodes staged in shared memory ([3][TPE]; lean record and
+  // correlation items outside the PML), or null.
+  const float *su;
 };
 
 // Correlation operands per point: the NREC record fields, then rho, cp, cs.
@@ -130,12 +133,18 @@ __device__ __forceinline__ void element_compute(const Consts &c, const Ptrs &p, 
       const float dtu = c.dt;
       float ux = 0.f, uy = 0.f, uz = 0.f;
       if (act) {
-        const size_t g =
-            (size_t)(ii * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
-        const float *U = p.u + (size_t)ev * 3 * c.G + g;
-        ux = __fadd_rn(U[0], __fmul_rn(dtu, vx));
-        uy = __fadd_rn(U[c.G], __fmul_rn(dtu, vy));
-        uz = __fadd_rn(U[2 * c.G], __fmul_rn(dtu, vz));
+        float u0, u1, u2;
+        if (x.su) {
+          u0 = x.su[n]; u1 = x.su[TPE + n]; u2 = x.su[2 * TPE + n];
+        } else {
+          const size_t g =
+              (size_t)(ii * 4 + in) + (size_t)c.GX * ((size_t)(j * 4 + jn) + (size_t)c.GY * (size_t)(k * 4 + kn));
+          const float *U = p.u + (size_t)ev * 3 * c.G + g;
+          u0 = U[0]; u1 = U[c.G]; u2 = U[2 * c.G];
+        }
+        ux = __fadd_rn(u0, __fmul_rn(dtu, vx));
+        uy = __fadd_rn(u1, __fmul_rn(dtu, vy));
+        uz = __fadd_rn(u2, __fmul_rn(dtu, vz));
       }
       s_p[0][n] = ux; s_p[1][n] = uy; s_p[2][n] = uz;
       __syncthreads();
@@ -518,7 +527,7 @@ __global__ void __launch_bounds__(TPE * EPB, (SES3D_ELEM_MINB / EPB > 0 ? SES3D_
   s_v[sub][0][n] = vx; s_v[sub][1][n] = vy; s_v[sub][2][n] = vz;
   __syncthreads();
   ElemCtx x{act, full, n, nn, in, jn, kn, ii, j, k, ev, e, N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2, cC, nullptr,
-            nullptr, false, -1};
+            nullptr, false, -1, nullptr};
   element_compute<DISS, MODE>(c, p, tab, s_v[sub], s_p[sub], x, sv);
 }
 
@@ -560,7 +569,14 @@ constexpr size_t TMA_SMEM = TMA_BAR_OFF + TMA_STAGES * sizeof(unsigned long long
 // Correlation iterations also stage their epilogue operands (CS_BYTES) behind the barriers.
 constexpr size_t TMA_CS_OFF = (TMA_SMEM + 15) / 16 * 16;
 __host__ __device__ constexpr bool tma_cstage(int mode) { return corr_mode(mode) && TMA_VBUF == 2; }
-__host__ __device__ constexpr size_t tma_smem(int mode) { return tma_cstage(mode) ? TMA_CS_OFF + CS_BYTES : TMA_SMEM; }
+// Lean record and correlation iterations also stage the displacement at the next item's
+// nodes, double-buffered like the velocity, behind that.
+__host__ __device__ constexpr bool tma_ustage(int mode) { return (mode == 4 || mode == 5) && TMA_VBUF == 2; }
+__host__ __device__ constexpr size_t tma_u_off(int mode) { return tma_cstage(mode) ? TMA_CS_OFF + CS_BYTES : TMA_CS_OFF; }
+__host__ __device__ constexpr size_t tma_smem(int mode) {
+  return tma_ustage(mode) ? tma_u_off(mode) + 2 * 3 * TPE * sizeof(float)
+                          : (tma_cstage(mode) ? TMA_CS_OFF + CS_BYTES : TMA_SMEM);
+}
 
 // Copies of one item into a stage. Byte ranges (element block of 18,000 B, fields of 500 B):
 // all 36 fields; elastic: fields 0-17 (9,008 B, the last 8 B inside field 18); lean outside
@@ -600,7 +616,7 @@ __device__ __forceinline__ void issue_item(const Consts &c, const Ptrs &p, long 
 // lean iterations; with the full state they cost more than the loads they replace.)
 template <bool TABLES>
 __device__ __forceinline__ void gather_v_async(const Consts &c, const Ptrs &p, long long item, float (*dst)[TPE],
-                                               float *lt, int n, int in, int jn, int kn) {
+                                               float *lt, int n, int in, int jn, int kn, float *udst = nullptr) {
   const int ev = (int)(item % c.nev);
   const unsigned e = (unsigned)(item / c.nev);
   const int i = (int)(e % (unsigned)c.ex), j = (int)((e / (unsigned)c.ex) % (unsigned)c.ey);
@@ -610,6 +626,11 @@ __device__ __forceinline__ void gather_v_async(const Consts &c, const Ptrs &p, l
     const float *v = p.v + (size_t)ev * 3 * c.G + g;
 #pragma unroll
     for (int q = 0; q < 3; ++q) cp_async4(&dst[q][n], v + (size_t)q * c.G);
+    if (udst && !in_pml_element(c, i, j, k)) {  // the displacement, read outside the PML only
+      const float *u = p.u + (size_t)ev * 3 * c.G + g;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) cp_async4(udst + q * TPE + n, u + (size_t)q * c.G);
+    }
   }
   if (!TABLES) {
   } else if (n < 5) {
@@ -680,7 +701,9 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
   const int nn = on ? n : 0;
   const int in = nn % 5, jn = (nn / 5) % 5, kn = nn / 25;
   constexpr bool TABLES = lean_mode(MODE);
-  if (TMA_VBUF == 2 && first < total) gather_v_async<TABLES>(c, p, first, s_vb, s_lt, n, in, jn, kn);
+  float *s_ub = nullptr;  // [2][3][TPE] displacement stages
+  if constexpr (tma_ustage(MODE)) s_ub = reinterpret_cast<float *>(smem + tma_u_off(MODE));
+  if (TMA_VBUF == 2 && first < total) gather_v_async<TABLES>(c, p, first, s_vb, s_lt, n, in, jn, kn, s_ub);
   // correlation operands: staged one item ahead, each thread its own point (cp.async groups
   // in the order velocity(t), operands(t), velocity(t + 1), operands(t + 1), ...)
   float *cstage = nullptr;
@@ -760,7 +783,7 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
     // previous item's divergence barrier
     if (TMA_VBUF == 2 && item + stride < total)
       gather_v_async<TABLES>(c, p, item + stride, s_vb + 3 * ((t + 1) % 2), s_lt + LT_FLOATS * ((t + 1) % 2), n, in,
-                             jn, kn);
+                             jn, kn, s_ub ? s_ub + 3 * TPE * ((t + 1) % 2) : nullptr);
     if constexpr (corr_mode(MODE))
       if (on && p.rec && item + stride < total) prefetch_corr<DISS>(c, p, item + stride, nn);
     const long long refill = item + TMA_STAGES * stride;
@@ -781,7 +804,8 @@ __global__ void __launch_bounds__(TPE, MINB) k_element_tma(const Consts c, const
     const float *lt = (TMA_VBUF == 2 && TABLES) ? s_lt + LT_FLOATS * (t % 2) : nullptr;
     const bool more = item + stride < total;
     ElemCtx x{on,  full, n,  nn, in, jn, kn, i, j, k, ev, e, (size_t)c.N, m0, S, vx, vy, vz, clam, c2mut, c2mt, cA, cB2,
-              cC,  lt,   cstage, TMA_VBUF == 2 && more, more ? item + stride : -1};
+              cC,  lt,   cstage, TMA_VBUF == 2 && more, more ? item + stride : -1,
+              s_ub ? s_ub + 3 * TPE * (t % 2) : nullptr};
     if (LATE_REFILL) element_compute<DISS, MODE>(c, p, *tab, s_v, s_p, x, sv, issue_refill);
     else element_compute<DISS, MODE>(c, p, *tab, s_v, s_p, x, sv);
   }
