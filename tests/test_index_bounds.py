@@ -109,3 +109,44 @@ def test_element_copy_ranges_inside_block():
             assert any(a <= lo and hi <= a + n for a, n in rs), (name, f)
     mat = 6 * 128 * 4
     assert block % 16 == 0 and mat % 16 == 0
+
+
+def test_element_shared_memory_layout():
+    """Dynamic shared memory of the persistent element kernel (kernels.cu: TMA_SMEM,
+    tma_smem): the stage of one item (state block and material), the velocity and pressure
+    buffers, the GLL tables, the 1-D table entries and the mbarrier; correlation items add
+    the staged epilogue operands (12 floats and up to 8 doubles per point), lean record and
+    correlation items two displacement stages. Every staged copy lands inside its buffer at
+    its natural alignment, and the resident CTAs each shape asks for fit the SM's 228 KB
+    (1 KB of it reserved per CTA)."""
+    TPE, VBUF = 128, 2
+    stage = 36 * 125 * 4 + 6 * 128 * 4                       # ElemStage, 16-byte aligned
+    ktab = ((25 * 3 + 25 + 25 * 3 + 5) * 4 + 15) // 16 * 16  # KTab rounded to 16 bytes
+    lt_off = stage + (9 + 3 * VBUF) * TPE * 4 + ktab
+    bar_off = lt_off + VBUF * 48 * 4
+    smem = bar_off + 8
+    assert bar_off % 8 == 0 and stage % 16 == 0
+    cs_off = (smem + 15) // 16 * 16
+    cs_bytes = 12 * 128 * 4 + 8 * 128 * 8
+    # staged operand addresses: floats [12][TPE], then doubles [8][TPE], thread n < 125
+    n = np.arange(125)
+    f_addr = cs_off + 4 * (np.arange(12)[:, None] * TPE + n[None, :])
+    d_addr = cs_off + 12 * TPE * 4 + 8 * (np.arange(8)[:, None] * TPE + n[None, :])
+    assert (f_addr % 4 == 0).all() and (d_addr % 8 == 0).all()
+    assert f_addr.max() + 4 <= cs_off + 12 * TPE * 4 and d_addr.max() + 8 <= cs_off + cs_bytes
+    sizes = {}
+    for mode in range(6):
+        corr, lean_rec = mode in (2, 5), mode in (4, 5)
+        u_off = cs_off + cs_bytes if corr else cs_off
+        size = u_off + 2 * 3 * TPE * 4 if lean_rec else (cs_off + cs_bytes if corr else smem)
+        if lean_rec:   # displacement stages [2][3][TPE] floats
+            u_addr = u_off + 4 * (np.arange(6)[:, None] * TPE + n[None, :])
+            assert u_off % 16 == 0 and u_addr.max() + 4 <= size
+        sizes[mode] = size
+    # resident CTAs per SM: full-state modes run shape 0 (5 CTAs), lean record and
+    # correlation modes shape 1 (4 CTAs), plain lean iterations every shape (up to 6)
+    per_sm = 228 * 1024
+    for mode, ctas in ((0, 6), (1, 5), (2, 5), (3, 6), (4, 4), (5, 4)):
+        assert ctas * (sizes[mode] + 1024) <= per_sm, (mode, sizes[mode])
+    # 44,208 B is the dynamic shared memory ncu reports for a MODE 2 launch
+    assert sizes[2] == 44208 and sizes[5] == 47280
